@@ -1,0 +1,225 @@
+"""Generate the golden fixtures by running the reference SlakoNet code.
+
+Run in a container that has the reference at ``/root/reference``:
+
+    python tests/golden/make_golden.py
+
+Every fixture is produced by the reference's own functions on seeded
+synthetic inputs from ``slakonet_gb300.synthetic``; the numbers are frozen
+as ``.npz`` files beside this script.  Tests compare the CPU oracle and the
+CUDA path against them; nothing at test time needs the reference.
+"""
+import os
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+from refharness import import_reference, build_reference_model  # noqa: E402
+from slakonet_gb300 import synthetic as syn  # noqa: E402
+
+ref = import_reference()
+torch.set_default_dtype(torch.float64)
+
+
+def tables_checksum(tables):
+    acc = []
+    for pk in sorted(tables["pairs"]):
+        for kind in ("H", "S"):
+            for key in sorted(tables["pairs"][pk][kind]):
+                t = tables["pairs"][pk][kind][key]
+                acc.append([np.abs(t).sum(), t[:, 100].sum(), t[:, -1].sum()])
+    for z in sorted(tables["elements"]):
+        acc.append([np.sum(tables["elements"][z]["on_sites"]), np.sum(tables["elements"][z]["occupations"]), 0.0])
+    return np.array(acc)
+
+
+def geometry(st):
+    return ref.atoms.Geometry(torch.tensor(st["numbers"]).unsqueeze(0),
+                              torch.tensor(st["positions"]).unsqueeze(0),
+                              cell=torch.tensor(st["cell"]).unsqueeze(0))
+
+
+class inject_kpoints:
+    """Replace ``Periodic._kpoints`` (slakonet/atoms.py:359-392) with a fixed list.
+
+    The reference's public API only builds offset Monkhorst-Pack grids or
+    k-lines; Gamma-centred grids are injected here.
+    """
+
+    def __init__(self, k):
+        self.k = torch.tensor(np.asarray(k, dtype=np.float64))
+
+    def __enter__(self):
+        P = ref.atoms.Periodic
+        self.orig = P._kpoints
+        k = self.k
+
+        def _kp(this, **kwargs):
+            nk = len(k)
+            return k.unsqueeze(0), torch.tensor([nk]), torch.full((1, nk), 1.0 / nk)
+        P._kpoints = _kp
+        return self
+
+    def __exit__(self, *a):
+        ref.atoms.Periodic._kpoints = self.orig
+
+
+def run_reference(model, st, shell_dict, kpoints=None, mesh=None, klines=None, keep_hs=None,
+                  extra_dos=None):
+    geom = geometry(st)
+    kw = dict(geometry=geom, shell_dict=shell_dict, device="cpu", get_fermi=True)
+    ctx = inject_kpoints(kpoints) if kpoints is not None else None
+    if mesh is not None:
+        kw["kpoints"] = torch.tensor(mesh)
+    if klines is not None:
+        kw["klines"] = torch.tensor(klines)
+    with torch.no_grad():
+        if ctx:
+            with ctx:
+                props, ok = model.compute_multi_element_properties(**kw)
+        else:
+            props, ok = model.compute_multi_element_properties(**kw)
+    calc = props["calc"]
+    out = {
+        "eigenvalues": props["eigenvalues"][0].numpy(),
+        "kpoints": calc.kpoints[0].numpy(),
+        "k_weights": calc.k_weights[0].numpy(),
+        "dos_energy_grid": props["dos_energy_grid_tensor"].numpy(),
+        "dos_values": props["dos_values_tensor"].numpy(),
+        "efermi_eV": props["efermi"].reshape(-1)[0].item(),
+        "bandgap_eV": props["bandgap"].reshape(-1)[0].item(),
+        "nelectrons": calc.nelectron.item(),
+    }
+    for key in ("fermi_energy_eV", "fermi_energy_Ha", "vbm_eV", "cbm_eV", "vbm_kpoint", "cbm_kpoint",
+                "valence_band_width_eV", "conduction_band_width_eV", "dos_at_fermi", "dos_gap_center_eV",
+                "dos_total_states", "nkpoints", "nbands"):
+        out[key] = np.float64(props[key])
+    out["band_gap_eV"] = float(props["band_gap_eV"])
+    out["is_direct_gap"] = bool(props["is_direct_gap"])
+    mdg = props["minimum_direct_gap_eV"]
+    out["minimum_direct_gap_eV"] = np.nan if mdg is None else float(mdg)
+    out["is_direct_semiconductor"] = bool(props["is_direct_semiconductor"])
+    if keep_hs is not None:
+        out["hk"] = calc.ham[0].permute(2, 0, 1)[keep_hs].numpy()
+        out["sk"] = calc.overlap[0].permute(2, 0, 1)[keep_hs].numpy()
+        out["hs_kindex"] = np.asarray(keep_hs)
+    if extra_dos is not None:
+        lo, hi, npts = extra_dos
+        with torch.no_grad():
+            g, d = calc.calculate_dos(energy_range=(lo, hi), num_points=npts, sigma=0.1)
+        out["dos2_grid"] = g.numpy()
+        out["dos2_values"] = d.numpy()
+    return out
+
+
+def fixture_interp():
+    rng = np.random.default_rng(11)
+    grid = syn.grid_points()
+    tab = rng.standard_normal((4, len(grid))).cumsum(1) * 0.01 * np.exp(-0.3 * grid)[None]
+    r = np.concatenate([rng.uniform(1e-3, 14.0, 400), [0.02, 0.1, 0.179, 13.2, 13.22, 13.24, 13.5, 14.0, 14.2, 14.23]])
+    pi = ref.interp.PolyInterpU(torch.tensor(grid), torch.tensor(tab.T))
+    vals = pi(torch.tensor(r)).numpy()
+    np.savez_compressed(os.path.join(HERE, "interp.npz"), table=tab, step=0.02, r=r, values=vals)
+
+
+def fixture_blocks():
+    rng = np.random.default_rng(12)
+    u = rng.standard_normal((64, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    # include axis-aligned and near-axis directions
+    u[:6] = [[0, 0, 1], [0, 0, -1], [1, 0, 0], [0, 1, 0], [0, -1, 0], [-1, 0, 0]]
+    u[6] = np.array([1e-9, 2e-9, 1.0]) / np.linalg.norm([1e-9, 2e-9, 1.0])
+    out = {"u": u}
+    for l1 in range(4):
+        for l2 in range(l1, 4):
+            ints = rng.standard_normal((64, l1 + 1))
+            blk = ref.sk.sub_block_rot(torch.tensor([l1, l2]), torch.tensor(u), torch.tensor(ints)).numpy()
+            out[f"ints_{l1}{l2}"] = ints
+            out[f"block_{l1}{l2}"] = blk
+    np.savez_compressed(os.path.join(HERE, "skblocks.npz"), **out)
+
+
+def save_case(name, tables, data, extra):
+    payload = dict(data)
+    payload.update(extra)
+    payload["tables_checksum"] = tables_checksum(tables)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **payload)
+
+
+def fixture_si_cfg0():
+    sd = {14: [0, 1, 2]}
+    tables = syn.make_tables([14], sd, seed=0)
+    model = build_reference_model(ref, tables)
+    st = syn.diamond_si()
+    data = run_reference(model, st, sd, mesh=[8, 8, 8], keep_hs=[0, 1, 77, 300, 511],
+                         extra_dos=(-20.0, 10.0, 1000))
+    save_case("si_cfg0", tables, data, {"numbers": st["numbers"], "positions": st["positions"],
+                                         "cell": st["cell"], "seed": 0, "shells": np.array([0, 1, 2])})
+
+
+def fixture_random(name, n_atoms, struct_seed, table_seed, zmax=65, mesh=None, numbers=None):
+    rng = np.random.default_rng(struct_seed)
+    st = syn.random_structure(rng, n_atoms, zmax=zmax)
+    if numbers is not None:
+        st["numbers"] = np.array(numbers)
+    sd_all = syn.default_shell_dict()
+    sd = {int(z): sd_all[int(z)] for z in st["numbers"]}
+    tables = syn.make_tables(st["numbers"], sd_all, seed=table_seed)
+    model = build_reference_model(ref, tables)
+    if mesh is None:
+        mesh = syn.gamma_centred_grid(st["cell"], n_atoms)
+    k = syn.gamma_centred_kpoints(mesh)
+    keep = sorted(set([0, len(k) // 2, len(k) - 1]))
+    data = run_reference(model, st, sd, kpoints=k, keep_hs=keep, extra_dos=(-20.0, 10.0, 1000))
+    save_case(name, tables, data, {"numbers": st["numbers"], "positions": st["positions"],
+                                    "cell": st["cell"], "mesh": np.array(mesh), "table_seed": table_seed})
+
+
+def fixture_klines():
+    sd = {14: [0, 1, 2]}
+    tables = syn.make_tables([14], sd, seed=0)
+    model = build_reference_model(ref, tables)
+    st = syn.diamond_si()
+    kl = np.array([[0.0, 0.0, 0.0, 0.5, 0.5, 0.0, 12],
+                   [0.5, 0.5, 0.0, 0.5, 0.25, 0.75, 7],
+                   [0.5, 0.25, 0.75, 0.0, 0.0, 0.0, 9]])
+    data = run_reference(model, st, sd, klines=kl)
+    save_case("si_klines", tables, data, {"numbers": st["numbers"], "positions": st["positions"],
+                                           "cell": st["cell"], "klines": kl, "seed": 0,
+                                           "shells": np.array([0, 1, 2])})
+
+
+def fixture_fermi():
+    """Reference ``fermi_search`` on assorted eigenvalue sets, including divergent ones."""
+    rng = np.random.default_rng(13)
+    cases = {}
+    for c in range(12):
+        nk, nb = int(rng.integers(1, 40)), int(rng.integers(2, 30))
+        eig = np.sort(rng.normal(-0.2, 0.3, (nk, nb)), axis=1)
+        if c % 3 == 1:
+            eig[:, nb // 2:] += 0.2   # gapped
+        w = np.full(nk, 1.0 / nk)
+        ne = float(rng.integers(1, 2 * nb))
+        mu = ref.fermi.fermi_search(torch.tensor(eig)[None], torch.tensor([ne]), torch.tensor(w)[None]).detach()
+        cases[f"eig_{c}"] = eig
+        cases[f"ne_{c}"] = np.float64(ne)
+        cases[f"mu_{c}"] = mu.reshape(-1)[0].item()
+    np.savez_compressed(os.path.join(HERE, "fermi.npz"), **cases)
+
+
+if __name__ == "__main__":
+    fixture_interp()
+    fixture_blocks()
+    fixture_fermi()
+    fixture_si_cfg0()
+    fixture_klines()
+    fixture_random("rand_f4", 4, 5, 3, numbers=[1, 26, 60, 33], mesh=(2, 2, 3))
+    fixture_random("rand_a", 6, 21, 21, zmax=30)
+    fixture_random("rand_b", 9, 22, 22)
+    fixture_random("rand_c", 3, 23, 23)
+    print("golden fixtures written to", HERE)
