@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 SlakoNet path: k-point eigensolves per second.
+
+Workload (one "step"): the uneven batch of 256 seeded random periodic
+structures, 2-64 atoms (log-uniform), elements Z = 1..65 with the default
+shell map (1/4/9/16 orbitals), triclinic cells, Gamma-centred k-grids at
+~1000 k-atoms, synthetic Slater-Koster tables for every element pair, and
+the whole path per structure: neighbour list, SK blocks, Bloch sums, FP64
+generalized eigensolve of every (structure, k), Fermi level, band gap and
+a 1000-point Gaussian DOS on [-20, 10] eV.
+
+``value`` times the kernels with inputs resident on the device; ``e2e``
+times the public batched API from host arrays (planning, host->device
+copies, kernels, device->host copy of eigenvalues, DOS and statistics).
+``--impl reference`` times the CPU oracle (the reference algorithm restated
+in numpy/LAPACK) on a stratified sample of the same workload with every
+host core.  Multi-GPU runs are independent replicas (the path does not
+shard across GPUs for this workload).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "k-pt eig solves/s"
+UNIT = "k-point solves/s"
+N_STRUCT = 256
+SEED = 0
+DOS_RANGE = (-20.0, 10.0)
+DOS_POINTS = 1000
+DOS_SIGMA = 0.1
+DOS_WINDOW = 9.0
+SAMPLE_STRIDE = 16         # CPU baseline: every 16th structure (stratified over sizes)
+WORKLOAD = ("uneven batch: 256 random periodic structures, 2-64 atoms log-uniform, Z=1-65 default shells, "
+            "Gamma-centred k-grids ~1000 k-atoms, FP64 generalized eigensolve per k, Fermi/gap, "
+            "1000-pt DOS on [-20,10] eV")
+
+
+def workload(n_struct=N_STRUCT, seed=SEED):
+    from slakonet_gb300 import synthetic as syn
+    sts = syn.uneven_batch(n_struct, seed=seed)
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    sd = syn.default_shell_dict()
+    tables = syn.make_tables(zs, sd, seed=seed)
+    for st in sts:
+        st["weights"] = np.full(len(st["kpoints"]), 1.0 / len(st["kpoints"]))
+    return sts, tables, sd
+
+
+def orbitals(st, sd):
+    return sum(sum(2 * l + 1 for l in sd[int(z)]) for z in st["numbers"])
+
+
+# --------------------------------------------------------------- CPU side
+
+def _oracle_one(args):
+    st, tables, sd = args
+    from oracle import slako_oracle as O
+    r = O.run_structure(st, tables, sd, st["kpoints"], st["weights"], dos_range=DOS_RANGE,
+                        dos_points=DOS_POINTS, dos_sigma=DOS_SIGMA)
+    return len(st["kpoints"])
+
+
+def _pool_init():
+    os.environ["OMP_NUM_THREADS"] = "1"
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    try:
+        from threadpoolctl import threadpool_limits
+        threadpool_limits(1)
+    except Exception:
+        pass
+
+
+def cpu_sample(sts, stride=SAMPLE_STRIDE):
+    order = sorted(range(len(sts)), key=lambda i: -len(sts[i]["numbers"]))
+    return [sts[i] for i in order[::stride]]
+
+
+def time_oracle(sample, tables, sd, pool, cores):
+    """Returns (solves, seconds) for one pass of the oracle over the sample."""
+    sub_tables = tables
+    t0 = time.perf_counter()
+    solves = sum(pool.imap_unordered(_oracle_one, [(st, sub_tables, sd) for st in sample], chunksize=1))
+    return solves, time.perf_counter() - t0
+
+
+def sub_tables_for(sample, tables):
+    zs = {int(z) for st in sample for z in st["numbers"]}
+    return {"grid": tables["grid"], "step": tables["step"],
+            "elements": {z: v for z, v in tables["elements"].items() if z in zs},
+            "pairs": {k: v for k, v in tables["pairs"].items() if k[0] in zs and k[1] in zs}}
+
+
+# --------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "0x1", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- GPU arm
+
+def fp64_peak(torch, lib, dev):
+    """Measured FP64 FMA throughput (TFLOP/s) with the library's probe kernel."""
+    from slakonet_gb300._lib import call, ptr
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, iters = sms * 8, 4096
+    out = torch.empty(blocks * 256, dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream().cuda_stream
+    call("skn_fp64_probe", ptr(out), blocks, iters, s)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        call("skn_fp64_probe", ptr(out), blocks, iters, s)
+        b.record()
+        torch.cuda.synchronize()
+        sec = a.elapsed_time(b) * 1e-3
+        best = max(best, 16.0 * iters * blocks * 256 / sec / 1e12)
+    return best
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from slakonet_gb300 import engine as E, model as M
+    import __graft_entry__ as ge
+    if rank == 0:
+        ge.build()
+    if world > 1:
+        torch.distributed.barrier()
+    ge.build()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    sts, tables, sd = workload(args.structures, args.seed)
+    model = M.MultiElementSkfParameterOptimizer.from_tables(tables)
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    ts = model.table_set(sd, dev, zs)
+    eng = E.Engine(ts)
+    plan = E.plan_batch(sts, ts)
+    db = E.DeviceBatch(plan, dev)
+    solves = int(plan.nk.sum())
+    flops_eig = float(sum((32.0 / 3.0) * float(n) ** 3 for n in plan.prob_n))
+    kw = dict(dos_range=DOS_RANGE, dos_points=DOS_POINTS, dos_sigma=DOS_SIGMA, dos_window=DOS_WINDOW)
+    for _ in range(args.warmup):
+        eng.execute(db, **kw)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # timed region: kernels only, inputs resident
+    eng.event_log = []
+    eng.launches = 0
+    with ClockSampler(dev.index) as clk:
+        barrier()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(args.steps):
+            res = eng.execute(db, **kw)
+        t1.record()
+        barrier()
+    elapsed = t0.elapsed_time(t1) * 1e-3
+    launches = eng.launches
+    per_call = {}
+    for name, a, b in eng.event_log:
+        per_call.setdefault(name, []).append(a.elapsed_time(b) * 1e-3)
+    eng.event_log = None
+    if world > 1:
+        t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    ok = int((res.eig_status == 0).sum().item())
+
+    # end-to-end through the public batched API from host arrays
+    e2e_times, h2d, d2h = [], 0, 0
+    barrier()
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = model.compute_properties_batch(sts, sd, dev, dos_range=DOS_RANGE, dos_points=DOS_POINTS,
+                                           dos_sigma=DOS_SIGMA, dos_window=DOS_WINDOW)
+        eig_h = r.eig.cpu()
+        dos_h = r.dos.cpu()
+        st_h = r.stats.cpu()
+        e2e_times.append(time.perf_counter() - t)
+        d2h = int(eig_h.numel() * 8 + dos_h.numel() * 8 + st_h.numel() * 8 + 4 * plan.n_pairs)
+        h2d = E.DeviceBatch(r.plan, dev).h2d_bytes() + 8 * (2 * plan.n_pairs + 1)
+    e2e = sum(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e = float(t.item())
+
+    peak = fp64_peak(torch, None, dev)
+    eig_t = statistics.mean(per_call["skn_eigh_gen_batched"])
+    achieved = flops_eig / eig_t / 1e12
+    shares = {k: round(sum(v) / elapsed, 4) for k, v in per_call.items()}
+    if rank != 0:
+        return None
+    out = {
+        "metric": METRIC, "value": world * solves * args.steps / elapsed, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "structures": args.structures, "seed": args.seed,
+                   "k_point_solves_per_step": solves, "max_n": int(plan.max_n),
+                   "mean_n": float(np.mean(plan.prob_n)), "eig_status_ok": ok,
+                   "l2": f"inputs larger than L2: H(k)+S(k) {2 * 16 * plan.hs_total / 1e9:.1f} GB per step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "tensor", "kernel": "k_eigh_gen (skn_eigh_gen_batched)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None,
+                     "peak_source": "measured in this run: FP64 FMA probe kernel (GB300 FP64 tensor MMA runs at "
+                                    "the same rate, so this is the FP64 roofline)",
+                     "algorithmic": "32/3 n^3 real flops per k (zpotrf 4/3 + zhegst 4 + zhetrd 16/3)",
+                     "eig_kernel_ms": eig_t * 1e3, "time_share": shares},
+        "e2e": {"value": world * solves * args.steps / e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e / args.steps},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    return out, sts, tables, sd
+
+
+def _single_thread_workers():
+    # spawned workers read these at numpy import: one BLAS thread per process
+    for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "BLIS_NUM_THREADS"):
+        os.environ[v] = "1"
+
+
+def run_cpu_baseline(sts, tables, sd, reps=1):
+    _single_thread_workers()
+    sample = cpu_sample(sts)
+    sub = sub_tables_for(sample, tables)
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_pool_init) as pool:
+        best = None
+        for _ in range(reps):
+            solves, sec = time_oracle(sample, sub, sd, pool, cores)
+            v = solves / sec
+            best = v if best is None else max(best, v)
+    return {"value": best, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"every {SAMPLE_STRIDE}th structure by size ({len(sample)} structures, {solves} k-point "
+                      f"solves, {sec:.1f} s), numpy/LAPACK oracle, one process per core"}
+
+
+def run_reference(args):
+    """CPU oracle arm: bounded stratified sample, all host cores, K timed steps after W warm-ups."""
+    sts, tables, sd = workload(args.structures, args.seed)
+    _single_thread_workers()
+    sample = cpu_sample(sts, SAMPLE_STRIDE * 2)
+    sub = sub_tables_for(sample, tables)
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_pool_init) as pool:
+        for _ in range(min(args.warmup, 1)):
+            time_oracle(sample[:4], sub, sd, pool, cores)
+        tot_s, tot_t = 0, 0.0
+        for _ in range(args.steps):
+            s, t = time_oracle(sample, sub, sd, pool, cores)
+            tot_s += s
+            tot_t += t
+    v = tot_s / tot_t
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "structures": args.structures, "seed": args.seed,
+                       "sample_structures": len(sample)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"every {2 * SAMPLE_STRIDE}th structure by size ({len(sample)} structures,"
+                                       f" {tot_s // max(args.steps, 1)} k-point solves per step)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--structures", type=int, default=N_STRUCT)
+    ap.add_argument("--seed", type=int, default=SEED)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    r = run_gpu(args, rank, world)
+    if rank == 0:
+        out, sts, tables, sd = r
+        if world == 1 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = run_cpu_baseline(sts, tables, sd)
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,195 @@
+/*
+ * slakonet_gb300.h -- C ABI of the GB300 (sm_103a) SlakoNet electronic-structure path.
+ *
+ * Every entry point takes raw device pointers owned by the caller, sizes, and
+ * a cudaStream_t; work is stream-ordered and the functions return an int
+ * status (SKN_OK == 0).  No entry point allocates device memory, throws, or
+ * synchronises the host unless its comment says so.  Per-problem numerical
+ * failures (S(k) not positive definite, NaN, no Fermi convergence) are
+ * reported in caller-provided status arrays, never as a failed call.
+ *
+ * Units: Bohr and Hartree; complex numbers are interleaved (re, im) doubles.
+ * Matrices are column-major, one n x n block per (structure, k) problem.
+ *
+ * Each declaration names the part of the reference SlakoNet code it
+ * replaces (paths relative to the reference project).
+ */
+#ifndef SLAKONET_GB300_H
+#define SLAKONET_GB300_H
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  SKN_OK = 0,
+  SKN_ERR_ARG = 1,          /* invalid argument (null pointer, bad size)          */
+  SKN_ERR_NOT_SPD = 2,      /* per-problem status: S(k) not positive definite      */
+  SKN_ERR_NAN = 3,          /* per-problem status: NaN met                         */
+  SKN_ERR_NO_CONVERGE = 4,  /* per-structure status: Fermi search hit max_iter     */
+  SKN_ERR_CAPACITY = 5,     /* request larger than the kernel's supported size     */
+  SKN_ERR_CUDA = 6          /* a CUDA launch or runtime call failed                */
+};
+
+/* Version of this ABI (major * 100 + minor). */
+int skn_abi_version(void);
+
+/* Maximum orbitals per atom (spdf = 16) and shells per atom supported. */
+#define SKN_MAX_ORB_PER_ATOM 16
+#define SKN_MAX_SHELLS 4
+/* Number of doubles per structure in the skn_fermi_gap statistics record. */
+#define SKN_NSTAT 24
+
+/*
+ * Bond counting.  Replaces the periodic image/distance tables of
+ * Periodic.get_cell_translations / _periodic_distance
+ * (slakonet/atoms.py:165-243) and the 0 < d < cutoff mask of hs_matrix
+ * (slakonet/slaterkoster.py:269-276).
+ *   atom_ptr[n_struct+1]   atoms of structure s are atom_ptr[s] .. atom_ptr[s+1)-1
+ *   positions[3*A]         Cartesian positions (Bohr)
+ *   cells[9*n_struct]      row-major lattice vectors (row i = vector i, Bohr)
+ *   image_range[3*n_struct] half widths r: translations T in [-r, r]^3
+ *   n_pairs                total ordered atom pairs, sum over structures of N_s^2
+ *   pair_base[n_struct]    first atom-pair slot of structure s (sum of N^2 before s)
+ *   pair_counts[n_pairs]   out: bonds of ordered pair (i, j) at pair_base[s] + i*N + j
+ */
+int skn_bond_counts(int n_struct, int64_t n_pairs, const int32_t* atom_ptr, const double* positions,
+                    const double* cells, const int32_t* image_range, double cutoff,
+                    const int64_t* pair_base, int32_t* pair_counts, cudaStream_t stream);
+
+/*
+ * Bond table fill: writes every directed bond (i, j, T) with 0 < d < cutoff,
+ * ordered by (structure, i, j, T with x slowest).  Same inputs as
+ * skn_bond_counts plus
+ *   pair_ptr[P]            exclusive scan of pair_counts (first bond of each pair)
+ *   pair_blk_base[P]       first block double of each pair's bonds
+ *   atom_norb[A]           orbitals per atom
+ * Outputs per bond: bond_i, bond_j (global atom index), bond_img (linear
+ * index of T in the structure's (2r+1)^3 box, x slowest), bond_d (Bohr),
+ * bond_u[3] (unit vector i -> j + T), bond_blk (offset of its real-space
+ * block, column-major norb_i x norb_j).
+ */
+int skn_bond_fill(int n_struct, int64_t n_pairs, const int32_t* atom_ptr, const double* positions,
+                  const double* cells, const int32_t* image_range, double cutoff,
+                  const int64_t* pair_base, const int64_t* pair_ptr, const int64_t* pair_blk_base,
+                  const int32_t* atom_norb, int32_t* bond_i, int32_t* bond_j, int32_t* bond_img,
+                  double* bond_d, double* bond_u, int64_t* bond_blk, cudaStream_t stream);
+
+/*
+ * Bloch phases exp(i 2 pi k . T) for every (k, T) of each structure's box.
+ * Replaces Periodic.phase (slakonet/atoms.py:543-558).
+ *   k_ptr[n_struct+1]      k-points of structure s are k_ptr[s] .. k_ptr[s+1)-1
+ *   kpoints[3*K]           fractional k
+ *   phase_base[n_struct]   first phase of structure s; layout [nk_s][n_img_s]
+ *   phases[2*...]          out, complex
+ */
+int skn_image_phases(int n_struct, const int32_t* image_range, const int32_t* k_ptr,
+                     const double* kpoints, const int64_t* phase_base, double* phases,
+                     cudaStream_t stream);
+
+/*
+ * Real-space Slater-Koster blocks H(R), S(R) for every bond: spline lookup
+ * of the integrals and rotation into the crystal frame.  Replaces
+ * _gather_off_site / SkfFeed.off_site / PolyInterpU (slakonet/slaterkoster.py:834-946,
+ * slakonet/skfeed.py:285-326, slakonet/interpolation.py:107-311) and
+ * sub_block_rot / sub_block_ref (slakonet/slaterkoster.py:1013-1122).
+ *   atom_species[A]        species index of each atom
+ *   sp_nshell[nsp], sp_shell_l[4*nsp], sp_norb[nsp]   shell layout per species
+ *   tab_index[16*nsp*nsp]  table of (spA, spB, l1, l2) at ((spA*nsp+spB)*4+l1)*4+l2, -1 if absent (l1 <= l2)
+ *   tab_off[ntab], tab_ngrid[ntab], tab_step[ntab]    table t: (l1+1) rows of tab_ngrid doubles
+ *                          at tab_H + tab_off[t] (and tab_S + tab_off[t]); row r is bond order r,
+ *                          column g the value at (g+1)*tab_step
+ *   blk_H, blk_S           out: real-space blocks at bond_blk[b]
+ *   status                 out (device int): SKN_ERR_ARG if a needed table is missing
+ */
+int skn_sk_blocks(int64_t n_bonds, const int32_t* bond_i, const int32_t* bond_j,
+                  const double* bond_d, const double* bond_u, const int64_t* bond_blk,
+                  const int32_t* atom_species, int n_species, const int32_t* sp_nshell,
+                  const int32_t* sp_shell_l, const int32_t* sp_norb, const int32_t* tab_index,
+                  const int64_t* tab_off, const int32_t* tab_ngrid, const double* tab_step,
+                  const double* tab_H, const double* tab_S, double* blk_H, double* blk_S,
+                  int32_t* status, cudaStream_t stream);
+
+/*
+ * Bloch sums H(k) = onsite + sum_T H(T) exp(i 2 pi k . T), same for S, as
+ * dense column-major matrices.  Replaces _pe_sk_data2 and the block scatter
+ * of hs_matrix (slakonet/slaterkoster.py:327-439, 971-1010).
+ * Problems p = (structure prob_struct[p], k index prob_k[p]) write
+ * n_s x n_s complex matrices at hs_off[p] (complex elements).
+ *   atom_ptr, pair_base, pair_ptr as above; orb_ptr[n_struct+1] orbital range of s;
+ *   orb_atom[n_orb_total]  local atom index of each orbital; atom_orb_off[A] first
+ *                          local orbital of each atom; atom_norb[A];
+ *   onsite_H[n_orb_total]  diagonal on-site energies (S gets 1)
+ */
+int skn_bloch(int n_prob, const int32_t* prob_struct, const int32_t* prob_k, const int64_t* hs_off,
+              const int32_t* atom_ptr, const int32_t* orb_ptr, const int32_t* orb_atom,
+              const int32_t* atom_orb_off, const int32_t* atom_norb, const int64_t* pair_base,
+              const int64_t* pair_ptr, const int32_t* bond_img, const int64_t* bond_blk,
+              const double* blk_H, const double* blk_S, const int32_t* image_range,
+              const int64_t* phase_base, const double* phases, const double* onsite_H,
+              int max_n, double* H, double* S, cudaStream_t stream);
+
+/*
+ * Batched generalized Hermitian eigenvalues H x = e S x, one problem per
+ * (structure, k).  Cholesky S = L L^H, reduction C = L^-1 H L^-H,
+ * Householder tridiagonalisation, Sturm bisection; FP64 throughout.
+ * Replaces eighb(..., scheme="chol") and the per-k loop of
+ * SimpleDftb.__call__ (slakonet/utils.py:741-783, slakonet/main.py:137-196).
+ *   n[p], hs_off[p], eig_off[p]  size and offsets of problem p
+ *   order[n_prob]          processing order (largest first is best)
+ *   H, S                   in/out: overwritten by the factorisations
+ *   eig                    out: ascending eigenvalues (Hartree) at eig_off[p]
+ *   status[p]              out: SKN_OK, SKN_ERR_NOT_SPD or SKN_ERR_NAN
+ *   work_counter           device int scratch, zeroed by the call (stream-ordered)
+ *   max_n                  largest n[p]
+ */
+int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                         const int32_t* order, double* H, double* S, double* eig, int32_t* status,
+                         int32_t* work_counter, int max_n, cudaStream_t stream);
+
+/*
+ * Fermi level, band gap and band-structure statistics per structure.
+ * Replaces fermi_search / fermi_dirac (slakonet/fermi.py:139-215),
+ * calculate_band_gap (slakonet/main.py:637-707),
+ * calculate_band_structure_properties (slakonet/main.py:1539-1642) and
+ * the get_fermi extras of compute_multi_element_properties (slakonet/optim.py:1011-1060).
+ *   eig_off[s], nk[s], nb[s]   eigenvalues [nk][nb] of structure s (ascending per k)
+ *   kw_off[s], kweights        k weights of structure s
+ *   nelec[s]                   electron count
+ *   mu[s] out; stats[SKN_NSTAT*s] out (layout in slakonet_gb300/engine.py STAT_*);
+ *   status[s] out: SKN_OK or SKN_ERR_NO_CONVERGE (NaN propagates as in the reference)
+ */
+int skn_fermi_gap(int n_struct, const int64_t* eig_off, const int32_t* nk, const int32_t* nb,
+                  const int64_t* kw_off, const double* kweights, const double* nelec, const double* eig,
+                  double kT, double tol, int max_iter, double* mu, double* stats, int32_t* status,
+                  cudaStream_t stream);
+
+/*
+ * Gaussian density of states on a uniform grid, energies shifted by the
+ * Fermi level and in eV.  Replaces calculate_dos and the DOS block of
+ * get_properties_dict (slakonet/main.py:709-797, 1766-1800).
+ * dos[s*npts + i] = sum_k w_k sum_b exp(-((E_i - (e_kb - mu_s) H2E)/sigma)^2/2)/(sigma sqrt(2 pi)).
+ * window_sigmas > 0 skips terms beyond that many sigmas (each skipped term
+ * is below exp(-window^2/2)); 0 sums every term.  Also fills grid[npts]
+ * and stats entries 16..18 (dos_at_fermi, gap centre, trapezoid total).
+ */
+int skn_dos(int n_struct, const int64_t* eig_off, const int32_t* nk, const int32_t* nb,
+            const int64_t* kw_off, const double* kweights, const double* eig, const double* mu,
+            double e_lo, double e_hi, int npts, double sigma, double window_sigmas,
+            double* grid, double* dos, double* stats, cudaStream_t stream);
+
+/*
+ * FP64 fused multiply-add throughput probe (no counterpart in the reference):
+ * blocks x 256 threads, 8 independent FMA chains of `iters` steps each,
+ * 16 * iters flops per thread, result written to out[blocks*256].  Used to
+ * measure the FP64 roofline the eigensolver is bound by.
+ */
+int skn_fp64_probe(double* out, int blocks, int iters, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SLAKONET_GB300_H */

@@ -1,0 +1,6 @@
+"""GB300-native SlakoNet electronic-structure path (sm_103a CUDA kernels behind a C ABI)."""
+from .model import Geometry, MultiElementSkfParameterOptimizer, SkfParameterOptimizer, properties_dict  # noqa: F401
+from .engine import Engine, TableSet, plan_batch  # noqa: F401
+
+__all__ = ["Geometry", "MultiElementSkfParameterOptimizer", "SkfParameterOptimizer", "Engine", "TableSet",
+           "plan_batch", "properties_dict"]

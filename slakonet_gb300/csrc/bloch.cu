@@ -1,0 +1,85 @@
+// Bloch sums: H(k) = onsite + sum_T H(T) exp(i 2 pi k.T), and S(k) alike.
+//
+// One CTA per (structure, k) problem; each warp takes ordered atom pairs
+// (i, j) and its lanes take the elements of the norb_i x norb_j block, so a
+// warp walks one bond list with uniform trip count: every lane reads the same
+// bond index and phase (broadcast) and its own block element (contiguous).
+// The reference builds the same sums with a phase multiply and scatter_add
+// over images followed by index scatters into [n, n, nk]
+// (slakonet/slaterkoster.py:327-439, 971-1010); here every element is
+// written once, k-major, column-major per k.
+#include "skn_common.cuh"
+
+namespace {
+
+__global__ void __launch_bounds__(256) k_bloch(
+    int n_prob, const int32_t* __restrict__ prob_struct, const int32_t* __restrict__ prob_k,
+    const int64_t* __restrict__ hs_off, const int32_t* __restrict__ atom_ptr, const int32_t* __restrict__ orb_ptr,
+    const int32_t* __restrict__ atom_orb_off, const int32_t* __restrict__ atom_norb,
+    const int64_t* __restrict__ pair_base, const int64_t* __restrict__ pair_ptr,
+    const int32_t* __restrict__ bond_img, const int64_t* __restrict__ bond_blk, const double* __restrict__ blk_H,
+    const double* __restrict__ blk_S, const int32_t* __restrict__ image_range,
+    const int64_t* __restrict__ phase_base, const double2* __restrict__ phases,
+    const double* __restrict__ onsite_H, double2* __restrict__ H, double2* __restrict__ S) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int p = blockIdx.x; p < n_prob; p += gridDim.x) {
+    const int s = prob_struct[p], k = prob_k[p];
+    const int a0 = atom_ptr[s], N = atom_ptr[s + 1] - a0;
+    const int o0 = orb_ptr[s], n = orb_ptr[s + 1] - o0;
+    const int nimg = (2 * image_range[3 * s] + 1) * (2 * image_range[3 * s + 1] + 1) * (2 * image_range[3 * s + 2] + 1);
+    const double2* ph = phases + phase_base[s] + (int64_t)k * nimg;
+    double2* Hp = H + hs_off[p];
+    double2* Sp = S + hs_off[p];
+    const int64_t pb = pair_base[s];
+    for (int q = wib; q < N * N; q += nw) {
+      const int ib = q / N, ia = q % N;  // consecutive warps: consecutive row blocks of one column block
+      const int gi = a0 + ia, gj = a0 + ib;
+      const int ni = atom_norb[gi], nj = atom_norb[gj];
+      const int oi = atom_orb_off[gi], oj = atom_orb_off[gj];
+      const int64_t t0 = pair_ptr[pb + (int64_t)ia * N + ib], t1 = pair_ptr[pb + (int64_t)ia * N + ib + 1];
+      for (int e = lane; e < ni * nj; e += 32) {
+        const int al = e % ni, bl = e / ni;
+        double2 h = make_double2(0.0, 0.0), sv = make_double2(0.0, 0.0);
+        for (int64_t t = t0; t < t1; ++t) {
+          const double2 f = ph[bond_img[t]];
+          const int64_t o = bond_blk[t] + e;
+          const double bh = blk_H[o], bs = blk_S[o];
+          h.x = fma(bh, f.x, h.x);
+          h.y = fma(bh, f.y, h.y);
+          sv.x = fma(bs, f.x, sv.x);
+          sv.y = fma(bs, f.y, sv.y);
+        }
+        if (ia == ib && al == bl) {
+          h.x += onsite_H[o0 + oi + al];
+          sv.x += 1.0;
+        }
+        const int64_t dst = (int64_t)(oj + bl) * n + (oi + al);
+        Hp[dst] = h;
+        Sp[dst] = sv;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int skn_bloch(int n_prob, const int32_t* prob_struct, const int32_t* prob_k, const int64_t* hs_off,
+                         const int32_t* atom_ptr, const int32_t* orb_ptr, const int32_t* orb_atom,
+                         const int32_t* atom_orb_off, const int32_t* atom_norb, const int64_t* pair_base,
+                         const int64_t* pair_ptr, const int32_t* bond_img, const int64_t* bond_blk,
+                         const double* blk_H, const double* blk_S, const int32_t* image_range,
+                         const int64_t* phase_base, const double* phases, const double* onsite_H,
+                         int max_n, double* H, double* S, cudaStream_t stream) {
+  (void)orb_atom;
+  (void)max_n;
+  if (n_prob < 0) return SKN_ERR_ARG;
+  if (n_prob == 0) return SKN_OK;
+  if (!prob_struct || !prob_k || !hs_off || !atom_ptr || !orb_ptr || !atom_orb_off || !atom_norb || !pair_base ||
+      !pair_ptr || !image_range || !phase_base || !phases || !onsite_H || !H || !S)
+    return SKN_ERR_ARG;
+  int blocks = n_prob < 152 * 8 ? n_prob : 152 * 8;
+  k_bloch<<<blocks, 256, 0, stream>>>(n_prob, prob_struct, prob_k, hs_off, atom_ptr, orb_ptr, atom_orb_off, atom_norb,
+                                      pair_base, pair_ptr, bond_img, bond_blk, blk_H, blk_S, image_range, phase_base,
+                                      (const double2*)phases, onsite_H, (double2*)H, (double2*)S);
+  return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
+}

@@ -1,0 +1,444 @@
+"""Host side of the GB300 path: parameter packing, batch planning, launches.
+
+``TableSet`` packs a model's per-element-pair tables (the reference's
+``Skf`` / ``SkfFeed`` data, slakonet/skf.py:152-199, slakonet/skfeed.py:560-739)
+into one device buffer with an index, so the kernels read every integral
+from HBM without the per-call Python feed.  ``plan_batch`` turns a list of
+structures into the flat descriptor arrays of the C ABI (CSR over atoms,
+atom pairs, k-points and (structure, k) problems).  ``Engine.run`` issues
+the kernels on one stream: bonds -> phases -> real-space blocks -> Bloch
+sums -> eigensolve -> Fermi/gap -> DOS.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import call, ptr
+
+H2E = 27.211
+CUTOFF_BOHR = 10.0          # hs_matrix default (slakonet/slaterkoster.py:111)
+KT_FERMI = 0.01             # fermi_search default (slakonet/fermi.py:143)
+
+# stats record layout (mirrors csrc/fermi_dos.cu)
+STAT = dict(mu_ha=0, fermi_ev=1, gap_ev=2, vbm_ev=3, cbm_ev=4, direct=5, vbm_k=6, cbm_k=7, vwidth=8,
+            cwidth=9, min_dgap=10, direct_semi=11, efermi_ev=12, bandgap_ev=13, converged=14, iters=15,
+            dos_fermi=16, dos_gapc=17, dos_total=18, metal=19, fallback=20)
+
+
+def _dev(device) -> torch.device:
+    d = torch.device(device)
+    if d.type != "cuda":
+        raise _lib.SknError("slakonet_gb300 runs on CUDA devices only (no CPU path)")
+    return d
+
+
+def _i32(a, device):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.int32)).to(device, non_blocking=True)
+
+
+def _i64(a, device):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.int64)).to(device, non_blocking=True)
+
+
+def _f64(a, device):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(device, non_blocking=True)
+
+
+# ------------------------------------------------------------------ tables
+
+class TableSet:
+    """Device-resident packed SK tables for a set of species.
+
+    ``h_tables[(za, zb)][(l1, l2)]`` / ``s_tables`` are tensors ``[l1+1, n_grid]``
+    (live parameters are accepted; they are read, not copied, when
+    ``requires_grad`` is off).  ``grids[(za, zb)]`` is the grid step,
+    ``onsite[z]`` the per-l on-site energies, ``occupations[z]`` per shell.
+    """
+
+    def __init__(self, species: Sequence[int], shell_dict: Dict[int, List[int]], h_tables, s_tables, steps,
+                 onsite, occupations, device):
+        self.device = torch.device(device)
+        self.species = [int(z) for z in sorted(set(int(z) for z in species))]
+        self.sp_of = {z: i for i, z in enumerate(self.species)}
+        nsp = len(self.species)
+        self.shell_dict = {z: list(shell_dict[z]) for z in self.species}
+        sp_nshell = np.zeros(nsp, np.int32)
+        sp_shell_l = np.zeros(4 * nsp, np.int32)
+        sp_norb = np.zeros(nsp, np.int32)
+        for i, z in enumerate(self.species):
+            ls = self.shell_dict[z]
+            if len(ls) > 4 or any(l < 0 or l > 3 for l in ls):
+                raise ValueError(f"at most 4 shells with l <= 3 per element, got {ls} for Z={z}")
+            sp_nshell[i] = len(ls)
+            sp_shell_l[4 * i: 4 * i + len(ls)] = ls
+            sp_norb[i] = sum(2 * l + 1 for l in ls)
+        tab_index = -np.ones(16 * nsp * nsp, np.int32)
+        offs, ngrid, stepv, hs, ss = [], [], [], [], []
+        off = 0
+        for a, za in enumerate(self.species):
+            for b, zb in enumerate(self.species):
+                if (za, zb) not in h_tables:
+                    continue
+                for (l1, l2), th in sorted(h_tables[(za, zb)].items()):
+                    ts = s_tables[(za, zb)][(l1, l2)]
+                    if l1 > l2 or l2 > 3:
+                        continue
+                    t = len(offs)
+                    tab_index[((a * nsp + b) * 4 + l1) * 4 + l2] = t
+                    if th.shape[-1] < 9:
+                        raise ValueError(f"table ({za},{zb},{l1},{l2}) has {th.shape[-1]} grid points; 9 needed")
+                    th = torch.as_tensor(th).detach().to(self.device, torch.float64)
+                    ts = torch.as_tensor(ts).detach().to(self.device, torch.float64)
+                    offs.append(off)
+                    ngrid.append(th.shape[-1])
+                    stepv.append(float(steps[(za, zb)]))
+                    hs.append(th.reshape(-1))
+                    ss.append(ts.reshape(-1))
+                    off += th.numel()
+        self.ntab = len(offs)
+        self.tab_H = torch.cat(hs) if hs else torch.zeros(1, dtype=torch.float64, device=self.device)
+        self.tab_S = torch.cat(ss) if ss else torch.zeros(1, dtype=torch.float64, device=self.device)
+        self.tab_index = _i32(tab_index, self.device)
+        self.tab_off = _i64(offs or [0], self.device)
+        self.tab_ngrid = _i32(ngrid or [0], self.device)
+        self.tab_step = _f64(stepv or [1.0], self.device)
+        self.sp_nshell = _i32(sp_nshell, self.device)
+        self.sp_shell_l = _i32(sp_shell_l, self.device)
+        self.sp_norb_np = sp_norb
+        self.sp_norb = _i32(sp_norb, self.device)
+        # per-species orbital on-site energies and electron counts
+        self.sp_onsite = []
+        self.sp_nelec = np.zeros(nsp)
+        for i, z in enumerate(self.species):
+            e = np.asarray(onsite[z], dtype=np.float64)
+            orb = []
+            for l in self.shell_dict[z]:
+                orb.extend([e[l]] * (2 * l + 1))
+            self.sp_onsite.append(np.array(orb))
+            self.sp_nelec[i] = float(np.sum(occupations[z]))
+
+    @classmethod
+    def from_synthetic(cls, tables: dict, shell_dict, device):
+        """From ``slakonet_gb300.synthetic.make_tables`` output."""
+        steps = {k: tables["step"] for k in tables["pairs"]}
+        h = {k: {kk: torch.as_tensor(vv) for kk, vv in v["H"].items()} for k, v in tables["pairs"].items()}
+        s = {k: {kk: torch.as_tensor(vv) for kk, vv in v["S"].items()} for k, v in tables["pairs"].items()}
+        onsite = {z: e["on_sites"] for z, e in tables["elements"].items()}
+        occ = {z: e["occupations"] for z, e in tables["elements"].items()}
+        species = sorted(tables["elements"].keys())
+        sd = {z: list(shell_dict[z]) for z in species}
+        return cls(species, sd, h, s, steps, onsite, occ, device)
+
+
+# ---------------------------------------------------------------- planning
+
+def image_range(cell: np.ndarray, positions: np.ndarray, cutoff: float) -> np.ndarray:
+    """Half-widths r of the translation box holding every bond shorter than cutoff.
+
+    |T_a| < cutoff |b_a| + spread_a, with b_a the reciprocal vectors (without
+    2 pi) and spread_a the extent of the fractional coordinates.
+    """
+    inv = np.linalg.inv(cell)
+    frac = positions @ inv
+    spread = frac.max(0) - frac.min(0) if len(frac) else np.zeros(3)
+    blen = np.linalg.norm(inv, axis=0)
+    return (np.floor(cutoff * blen + spread) + 1).astype(np.int32)
+
+
+@dataclass
+class Plan:
+    n_struct: int
+    numbers: List[np.ndarray]
+    atom_ptr: np.ndarray
+    orb_ptr: np.ndarray
+    positions: np.ndarray
+    cells: np.ndarray
+    image_range: np.ndarray
+    atom_species: np.ndarray
+    atom_norb: np.ndarray
+    atom_orb_off: np.ndarray
+    orb_atom: np.ndarray
+    onsite_H: np.ndarray
+    pair_base: np.ndarray
+    n_pairs: int
+    pair_ni_nj: np.ndarray
+    k_ptr: np.ndarray
+    kpoints: np.ndarray
+    kweights: np.ndarray
+    kw_off: np.ndarray
+    nk: np.ndarray
+    nb: np.ndarray
+    phase_base: np.ndarray
+    n_phase: int
+    prob_struct: np.ndarray
+    prob_k: np.ndarray
+    prob_n: np.ndarray
+    hs_off: np.ndarray
+    hs_total: int
+    eig_off_prob: np.ndarray
+    eig_off_struct: np.ndarray
+    eig_total: int
+    order: np.ndarray
+    nelec: np.ndarray
+    max_n: int
+
+
+def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUTOFF_BOHR) -> Plan:
+    """Flat descriptors for a batch.  Each structure: numbers, positions (Bohr),
+    cell (Bohr, rows = lattice vectors), kpoints [nk,3] fractional, optional weights."""
+    S = len(structures)
+    atom_ptr = np.zeros(S + 1, np.int32)
+    orb_ptr = np.zeros(S + 1, np.int32)
+    k_ptr = np.zeros(S + 1, np.int32)
+    pos, cells, rng, species, norb, aoff, oatom, onsite = [], [], [], [], [], [], [], []
+    kp, kw, nums, nelec = [], [], [], np.zeros(S)
+    pair_base = np.zeros(S, np.int64)
+    phase_base = np.zeros(S, np.int64)
+    nk = np.zeros(S, np.int32)
+    nb = np.zeros(S, np.int32)
+    pb = 0
+    phb = 0
+    ninj = []
+    for s, st in enumerate(structures):
+        z = np.asarray(st["numbers"], dtype=np.int64).reshape(-1)
+        p = np.asarray(st["positions"], dtype=np.float64).reshape(-1, 3)
+        c = np.asarray(st["cell"], dtype=np.float64).reshape(3, 3)
+        k = np.asarray(st["kpoints"], dtype=np.float64).reshape(-1, 3)
+        w = np.asarray(st.get("weights", np.full(len(k), 1.0 / max(len(k), 1))), dtype=np.float64)
+        try:
+            sp = np.array([tables.sp_of[int(a)] for a in z], np.int32)
+        except KeyError as e:
+            raise ValueError(f"no parameters for element Z={e.args[0]}") from None
+        no = tables.sp_norb_np[sp]
+        N = len(z)
+        atom_ptr[s + 1] = atom_ptr[s] + N
+        orb_ptr[s + 1] = orb_ptr[s] + int(no.sum())
+        k_ptr[s + 1] = k_ptr[s] + len(k)
+        pos.append(p)
+        cells.append(c)
+        r = image_range(c, p, cutoff)
+        rng.append(r)
+        species.append(sp)
+        norb.append(no)
+        off = np.concatenate([[0], np.cumsum(no)[:-1]]).astype(np.int32)
+        aoff.append(off)
+        oatom.append(np.repeat(np.arange(N, dtype=np.int32), no))
+        onsite.append(np.concatenate([tables.sp_onsite[q] for q in sp]))
+        kp.append(k)
+        kw.append(w)
+        nums.append(z)
+        nelec[s] = float(tables.sp_nelec[sp].sum())
+        pair_base[s] = pb
+        pb += N * N
+        ninj.append(np.outer(no, no).reshape(-1))
+        nimg = int(np.prod(2 * r + 1))
+        phase_base[s] = phb
+        phb += nimg * len(k)
+        nk[s] = len(k)
+        nb[s] = int(no.sum())
+    prob_struct = np.repeat(np.arange(S, dtype=np.int32), nk)
+    prob_k = np.concatenate([np.arange(n, dtype=np.int32) for n in nk]) if S else np.zeros(0, np.int32)
+    prob_n = nb[prob_struct]
+    sz = prob_n.astype(np.int64) ** 2
+    hs_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
+    eig_sz = nk.astype(np.int64) * nb
+    eig_off_struct = np.concatenate([[0], np.cumsum(eig_sz)[:-1]]).astype(np.int64)
+    eig_off_prob = eig_off_struct[prob_struct] + prob_k.astype(np.int64) * prob_n
+    order = np.argsort(-prob_n, kind="stable").astype(np.int32)
+    kw_off = k_ptr[:-1].astype(np.int64)
+    return Plan(S, nums, atom_ptr, orb_ptr, np.concatenate(pos), np.stack(cells), np.stack(rng),
+                np.concatenate(species), np.concatenate(norb).astype(np.int32), np.concatenate(aoff),
+                np.concatenate(oatom), np.concatenate(onsite), pair_base, int(pb),
+                np.concatenate(ninj).astype(np.int64), k_ptr, np.concatenate(kp), np.concatenate(kw), kw_off,
+                nk, nb, phase_base, int(phb), prob_struct, prob_k, prob_n, hs_off, int(sz.sum()),
+                eig_off_prob, eig_off_struct, int(eig_sz.sum()), order, nelec, int(nb.max()) if S else 0)
+
+
+# ------------------------------------------------------------------ engine
+
+@dataclass
+class BatchResult:
+    plan: Plan
+    eig: torch.Tensor            # flat eigenvalues, structure s at eig_off_struct[s], [nk][nb]
+    eig_status: torch.Tensor     # per problem
+    mu: torch.Tensor             # per structure (Hartree)
+    stats: torch.Tensor          # [S, SKN_NSTAT]
+    fermi_status: torch.Tensor
+    dos_grid: torch.Tensor
+    dos: torch.Tensor            # [S, npts]
+    H: Optional[torch.Tensor] = None
+    S: Optional[torch.Tensor] = None
+    timings: dict = field(default_factory=dict)
+
+    def eigenvalues(self, s: int) -> torch.Tensor:
+        p = self.plan
+        o = int(p.eig_off_struct[s])
+        return self.eig[o: o + int(p.nk[s]) * int(p.nb[s])].view(int(p.nk[s]), int(p.nb[s]))
+
+
+class DeviceBatch:
+    """A planned batch with its descriptor arrays resident on the device."""
+
+    def __init__(self, plan: Plan, device):
+        dev = device
+        self.plan = plan
+        self.atom_ptr = _i32(plan.atom_ptr, dev)
+        self.pos = _f64(plan.positions, dev)
+        self.cells = _f64(plan.cells, dev)
+        self.rng = _i32(plan.image_range, dev)
+        self.pair_base = _i64(plan.pair_base, dev)
+        self.norb = _i32(plan.atom_norb, dev)
+        self.kptr = _i32(plan.k_ptr, dev)
+        self.kp = _f64(plan.kpoints, dev)
+        self.phb = _i64(plan.phase_base, dev)
+        self.species = _i32(plan.atom_species, dev)
+        self.ps = _i32(plan.prob_struct, dev)
+        self.pk = _i32(plan.prob_k, dev)
+        self.hs_off = _i64(plan.hs_off, dev)
+        self.orb_ptr = _i32(plan.orb_ptr, dev)
+        self.orb_atom = _i32(plan.orb_atom, dev)
+        self.aoff = _i32(plan.atom_orb_off, dev)
+        self.onsite = _f64(plan.onsite_H, dev)
+        self.n = _i32(plan.prob_n, dev)
+        self.eoff = _i64(plan.eig_off_prob, dev)
+        self.order = _i32(plan.order, dev)
+        self.eos = _i64(plan.eig_off_struct, dev)
+        self.nk = _i32(plan.nk, dev)
+        self.nb = _i32(plan.nb, dev)
+        self.kwoff = _i64(plan.kw_off, dev)
+        self.kw = _f64(plan.kweights, dev)
+        self.ne = _f64(plan.nelec, dev)
+
+    def h2d_bytes(self) -> int:
+        return sum(int(v.numel() * v.element_size()) for v in vars(self).values() if isinstance(v, torch.Tensor))
+
+
+# kernels each ABI call launches (for the launch count the bench reports)
+KERNELS_PER_CALL = {"skn_bond_counts": 1, "skn_bond_fill": 1, "skn_image_phases": 1, "skn_sk_blocks": 1,
+                    "skn_bloch": 1, "skn_eigh_gen_batched": 1, "skn_fermi_gap": 1, "skn_dos": 2}
+
+
+class Engine:
+    """Runs the whole path for a planned batch on one CUDA stream."""
+
+    def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None):
+        _dev(tables.device)
+        self.tables = tables
+        self.cutoff = float(cutoff)
+        self.device = tables.device
+        self.stream = stream
+        self.launches = 0
+        self.event_log = None   # set to a list to record (name, start, end) CUDA events per call
+
+    def _call(self, name, *args):
+        ev = self.event_log
+        if ev is not None:
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+        call(name, *args)
+        if ev is not None:
+            b.record()
+            ev.append((name, a, b))
+        self.launches += KERNELS_PER_CALL.get(name, 1)
+
+    def run(self, plan: Plan, dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
+            dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False) -> BatchResult:
+        with torch.cuda.device(self.device):
+            ctx = torch.cuda.stream(self.stream) if self.stream is not None else _nullctx()
+            with ctx:
+                db = DeviceBatch(plan, self.device)
+                return self.execute(db, dos_range, dos_points, dos_sigma, dos_window, keep_hs, hs_only)
+
+    def execute(self, db: DeviceBatch, dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
+                dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False) -> BatchResult:
+        """Kernels only, on the current stream; one device->host read sizes the bond table."""
+        plan = db.plan
+        dev = self.device
+        T = self.tables
+        S = plan.n_struct
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        counts = torch.empty(max(plan.n_pairs, 1), dtype=torch.int32, device=dev)
+        self._call("skn_bond_counts", S, plan.n_pairs, ptr(db.atom_ptr), ptr(db.pos), ptr(db.cells), ptr(db.rng),
+                   self.cutoff, ptr(db.pair_base), ptr(counts), stream)
+        cnt = counts[: plan.n_pairs].to("cpu").numpy().astype(np.int64)   # sizes the bond table (one sync)
+        pair_ptr = np.zeros(plan.n_pairs + 1, np.int64)
+        np.cumsum(cnt, out=pair_ptr[1:])
+        pair_blk = np.zeros(plan.n_pairs + 1, np.int64)
+        np.cumsum(cnt * plan.pair_ni_nj, out=pair_blk[1:])
+        nbond = int(pair_ptr[-1])
+        nblk = int(pair_blk[-1])
+        d_pair_ptr = _i64(pair_ptr, dev)
+        d_pair_blk = _i64(pair_blk[:-1] if plan.n_pairs else np.zeros(1), dev)
+        nb1 = max(nbond, 1)
+        bond_i = torch.empty(nb1, dtype=torch.int32, device=dev)
+        bond_j = torch.empty(nb1, dtype=torch.int32, device=dev)
+        bond_img = torch.empty(nb1, dtype=torch.int32, device=dev)
+        bond_d = torch.empty(nb1, dtype=torch.float64, device=dev)
+        bond_u = torch.empty(3 * nb1, dtype=torch.float64, device=dev)
+        bond_blk = torch.empty(nb1, dtype=torch.int64, device=dev)
+        self._call("skn_bond_fill", S, plan.n_pairs, ptr(db.atom_ptr), ptr(db.pos), ptr(db.cells), ptr(db.rng),
+                   self.cutoff, ptr(db.pair_base), ptr(d_pair_ptr), ptr(d_pair_blk), ptr(db.norb), ptr(bond_i),
+                   ptr(bond_j), ptr(bond_img), ptr(bond_d), ptr(bond_u), ptr(bond_blk), stream)
+        phases = torch.empty(2 * max(plan.n_phase, 1), dtype=torch.float64, device=dev)
+        self._call("skn_image_phases", S, ptr(db.rng), ptr(db.kptr), ptr(db.kp), ptr(db.phb), ptr(phases), stream)
+        blk_H = torch.empty(max(nblk, 1), dtype=torch.float64, device=dev)
+        blk_S = torch.empty(max(nblk, 1), dtype=torch.float64, device=dev)
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        if nbond:
+            self._call("skn_sk_blocks", nbond, ptr(bond_i), ptr(bond_j), ptr(bond_d), ptr(bond_u), ptr(bond_blk),
+                       ptr(db.species), len(T.species), ptr(T.sp_nshell), ptr(T.sp_shell_l), ptr(T.sp_norb),
+                       ptr(T.tab_index), ptr(T.tab_off), ptr(T.tab_ngrid), ptr(T.tab_step), ptr(T.tab_H),
+                       ptr(T.tab_S), ptr(blk_H), ptr(blk_S), ptr(status), stream)
+        n_prob = len(plan.prob_n)
+        Hk = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
+        Sk = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
+        self._call("skn_bloch", n_prob, ptr(db.ps), ptr(db.pk), ptr(db.hs_off), ptr(db.atom_ptr), ptr(db.orb_ptr),
+                   ptr(db.orb_atom), ptr(db.aoff), ptr(db.norb), ptr(db.pair_base), ptr(d_pair_ptr), ptr(bond_img),
+                   ptr(bond_blk), ptr(blk_H), ptr(blk_S), ptr(db.rng), ptr(db.phb), ptr(phases), ptr(db.onsite),
+                   plan.max_n, ptr(Hk), ptr(Sk), stream)
+        self._status = status
+        hs_copy = (Hk.clone(), Sk.clone()) if keep_hs else (None, None)
+        if hs_only:
+            self.check_tables()
+            return BatchResult(plan, None, None, None, None, None, None, None, hs_copy[0], hs_copy[1])
+        eig = torch.empty(max(plan.eig_total, 1), dtype=torch.float64, device=dev)
+        eig_status = torch.empty(max(n_prob, 1), dtype=torch.int32, device=dev)
+        counter = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._call("skn_eigh_gen_batched", n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order), ptr(Hk),
+                   ptr(Sk), ptr(eig), ptr(eig_status), ptr(counter), plan.max_n, stream)
+        mu = torch.empty(S, dtype=torch.float64, device=dev)
+        stats = torch.zeros(S * _lib.SKN_NSTAT, dtype=torch.float64, device=dev)
+        fst = torch.empty(S, dtype=torch.int32, device=dev)
+        self._call("skn_fermi_gap", S, ptr(db.eos), ptr(db.nk), ptr(db.nb), ptr(db.kwoff), ptr(db.kw), ptr(db.ne),
+                   ptr(eig), KT_FERMI, 1e-6, 100, ptr(mu), ptr(stats), ptr(fst), stream)
+        grid = torch.empty(dos_points, dtype=torch.float64, device=dev)
+        dos = torch.empty(S * dos_points, dtype=torch.float64, device=dev)
+        self._call("skn_dos", S, ptr(db.eos), ptr(db.nk), ptr(db.nb), ptr(db.kwoff), ptr(db.kw), ptr(eig), ptr(mu),
+                   float(dos_range[0]), float(dos_range[1]), int(dos_points), float(dos_sigma), float(dos_window),
+                   ptr(grid), ptr(dos), ptr(stats), stream)
+        return BatchResult(plan, eig, eig_status, mu, stats.view(S, _lib.SKN_NSTAT), fst, grid,
+                           dos.view(S, dos_points), hs_copy[0], hs_copy[1])
+
+    def check_tables(self):
+        """Raise if the last execute() needed a table the parameter set lacks (reads one device int)."""
+        if int(self._status.item()) != 0:
+            raise _lib.SknError("sk_blocks: a Slater-Koster table needed by this structure is missing")
+
+
+class _nullctx:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def C_stream(st: torch.cuda.Stream):
+    return st.cuda_stream

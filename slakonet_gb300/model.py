@@ -1,0 +1,337 @@
+"""Drop-in model API: ``MultiElementSkfParameterOptimizer.compute_multi_element_properties``.
+
+Mirrors the reference's model object (slakonet/optim.py:139-1443): a
+``ModuleDict`` ``skf_optimizers`` keyed ``"A-B"`` by element symbols, each a
+``SkfParameterOptimizer`` with ``h_params`` / ``s_params`` ParameterDicts
+keyed ``"l1-l2"`` holding FP64 tensors ``[l1+1, n_grid]``.  State-dict keys
+are therefore the reference's ``skf_optimizers.A-B.h_params.l1-l2``.
+
+``compute_multi_element_properties`` keeps the reference signature and
+returns the same ``(properties, True)`` pair (slakonet/optim.py:949-1075,
+slakonet/main.py:1657-1819); the numbers come from the CUDA path in
+``engine.py``.  There is no CPU path: a non-CUDA device raises.
+"""
+from __future__ import annotations
+
+import types
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+import torch
+import torch.nn as nn
+
+from . import engine as E
+from .elements import SYMBOLS, symbol_to_z
+
+H2E = 27.211
+
+
+class Geometry:
+    """Minimal periodic geometry with the reference's attribute layout.
+
+    ``atomic_numbers [1, N]``, ``positions [1, N, 3]`` and ``cell [1, 3, 3]``
+    in Bohr (rows of ``cell`` are lattice vectors), as ``slakonet.atoms.Geometry``
+    (slakonet/atoms.py:573-700).  Any object with these attributes is accepted
+    by ``compute_multi_element_properties``.
+    """
+
+    _LEN = {"bohr": 1.0, "angstrom": 1.0 / 0.529177249}
+
+    def __init__(self, atomic_numbers, positions, cell=None, units: str = "bohr"):
+        f = self._LEN[units.lower()]
+        z = torch.as_tensor(atomic_numbers).reshape(1, -1)
+        p = torch.as_tensor(positions, dtype=torch.float64).reshape(1, -1, 3) * f
+        self.atomic_numbers = z
+        self.positions = p
+        self.cell = None if cell is None else torch.as_tensor(cell, dtype=torch.float64).reshape(1, 3, 3) * f
+        self.is_periodic = cell is not None
+
+    @property
+    def n_atoms(self):
+        return self.atomic_numbers.count_nonzero(-1)
+
+
+def _structure_from_geometry(geometry) -> dict:
+    z = torch.as_tensor(geometry.atomic_numbers).detach().cpu().reshape(-1).numpy()
+    pos = torch.as_tensor(geometry.positions).detach().cpu().reshape(-1, 3).numpy()
+    cell = getattr(geometry, "cell", None)
+    if cell is None:
+        raise ValueError("a periodic geometry with a cell is required")
+    cell = torch.as_tensor(cell).detach().cpu().reshape(3, 3).numpy()
+    keep = z != 0
+    return {"numbers": z[keep].astype(np.int64), "positions": pos[keep].astype(np.float64),
+            "cell": cell.astype(np.float64)}
+
+
+def mp_kpoints(mesh) -> np.ndarray:
+    """Offset Monkhorst-Pack grid ``0.5/n + i/n`` (slakonet/atoms.py:394-446), x slowest."""
+    n1, n2, n3 = (int(v) for v in np.asarray(mesh).reshape(-1)[:3])
+    a = 0.5 / n1 + np.arange(n1) * (1.0 / n1)
+    b = 0.5 / n2 + np.arange(n2) * (1.0 / n2)
+    c = 0.5 / n3 + np.arange(n3) * (1.0 / n3)
+    return np.stack(np.meshgrid(a, b, c, indexing="ij"), -1).reshape(-1, 3)
+
+
+def klines_kpoints(klines) -> np.ndarray:
+    """Band-path points ``k1 + i (k2-k1)/(N-1)`` per segment (slakonet/atoms.py:448-502)."""
+    kl = np.asarray(torch.as_tensor(klines).detach().cpu().numpy(), dtype=np.float64).reshape(-1, 7)
+    pts = []
+    for row in kl:
+        n = int(row[6])
+        d = row[3:6] - row[0:3]
+        if n >= 1:
+            with np.errstate(divide="ignore", invalid="ignore"):
+                d = d / (row[6] - 1.0)
+        pts.extend(row[0:3] + d * i for i in range(n))
+    return np.array(pts, dtype=np.float64).reshape(-1, 3)
+
+
+class SkfParameterOptimizer(nn.Module):
+    """Trainable tables of one element pair (slakonet/optim.py:1356-1443)."""
+
+    def __init__(self, atom_pair: Sequence[int], h: Dict[str, torch.Tensor], s: Dict[str, torch.Tensor],
+                 grid, atomic_data: Optional[dict] = None, hs_cutoff=None):
+        super().__init__()
+        self.h_params = nn.ParameterDict({k: nn.Parameter(torch.as_tensor(v, dtype=torch.float64).clone())
+                                          for k, v in h.items()})
+        self.s_params = nn.ParameterDict({k: nn.Parameter(torch.as_tensor(v, dtype=torch.float64).clone())
+                                          for k, v in s.items()})
+        self.original_h_params = {k: v.detach().clone() for k, v in self.h_params.items()}
+        self.original_s_params = {k: v.detach().clone() for k, v in self.s_params.items()}
+        self.atom_pair = [int(atom_pair[0]), int(atom_pair[1])]
+        self.grid = [float(g) for g in np.asarray(grid).reshape(-1)]
+        self.atomic_data = atomic_data
+        self.hs_cutoff = hs_cutoff if hs_cutoff is not None else self.grid[-1]
+        self.skf_dict = {"atom_pair": self.atom_pair, "grid": self.grid, "hs_cutoff": self.hs_cutoff,
+                         "atomic": atomic_data is not None}
+        if atomic_data is not None:
+            self.skf_dict["atomic_data"] = atomic_data
+
+    @property
+    def grid_step(self) -> float:
+        return self.grid[1] - self.grid[0]
+
+    def apply_constraints(self, c=(0.9, 0.7, 0.95, 0.9)):
+        """Clamp parameters to a band around their initial values (slakonet/optim.py:1392-1434)."""
+        with torch.no_grad():
+            for key, p in self.h_params.items():
+                o = self.original_h_params[key].to(p.device)
+                f = c[0] if key.split("-")[0] == key.split("-")[1] else c[1]
+                p.data = torch.clamp(p.data, o * f, o * (1 + (1 - f)))
+            for key, p in self.s_params.items():
+                o = self.original_s_params[key].to(p.device)
+                if key.split("-")[0] == key.split("-")[1]:
+                    p.data = torch.clamp(p.data, torch.maximum(o * c[2], torch.tensor(0.1, dtype=o.dtype,
+                                                                                     device=o.device)),
+                                         o * (1 + (1 - c[2])))
+                else:
+                    p.data = torch.clamp(p.data, o * c[3], o * (1 + (1 - c[3])))
+
+
+class MultiElementSkfParameterOptimizer(nn.Module):
+    """Model object with the reference's parameter layout and property API."""
+
+    def __init__(self):
+        super().__init__()
+        self.skf_optimizers = nn.ModuleDict()
+        self.atomic_num_to_symbol = {z: SYMBOLS[z] for z in range(1, len(SYMBOLS))}
+        self._table_cache = None
+
+    # ------------------------------------------------------------ building
+    @classmethod
+    def from_tables(cls, tables: dict) -> "MultiElementSkfParameterOptimizer":
+        """From ``synthetic.make_tables`` output (grid, per-pair H/S, element data)."""
+        m = cls()
+        for (za, zb), pair in sorted(tables["pairs"].items()):
+            h = {f"{l1}-{l2}": v for (l1, l2), v in pair["H"].items()}
+            s = {f"{l1}-{l2}": v for (l1, l2), v in pair["S"].items()}
+            atomic = None
+            if za == zb:
+                el = tables["elements"][za]
+                atomic = {"on_sites": [float(x) for x in el["on_sites"]],
+                          "hubbard_us": [0.0] * len(el["on_sites"]), "mass": 1.0,
+                          "occupations": [float(x) for x in el["occupations"]]}
+            m.skf_optimizers[f"{SYMBOLS[za]}-{SYMBOLS[zb]}"] = SkfParameterOptimizer(
+                (za, zb), h, s, tables["grid"], atomic)
+        return m
+
+    @classmethod
+    def load_ultra_compact(cls, path: str) -> "MultiElementSkfParameterOptimizer":
+        """Read the reference's ultra-compact checkpoint (slakonet/optim.py:528-625).
+
+        The file holds ``metadata`` (``available_pairs``), ``skf_metadata``
+        (grid, atomic data per pair) and ``trained_parameters`` (a state dict
+        with ``skf_optimizers.A-B.{h,s}_params.l1-l2`` keys).
+        """
+        data = torch.load(path, map_location="cpu", weights_only=False)
+        meta, sd, skm = data["metadata"], data["trained_parameters"], data["skf_metadata"]
+        m = cls()
+        for pk in meta["available_pairs"]:
+            h, s = {}, {}
+            for key, v in sd.items():
+                if key.startswith(f"skf_optimizers.{pk}.h_params."):
+                    h[key.split(".")[-1]] = v
+                elif key.startswith(f"skf_optimizers.{pk}.s_params."):
+                    s[key.split(".")[-1]] = v
+            md = skm[pk]
+            m.skf_optimizers[pk] = SkfParameterOptimizer(md["atom_pair"], h, s, md["grid"], md.get("atomic_data"),
+                                                         md.get("hs_cutoff"))
+        m.load_state_dict(sd, strict=False)
+        return m
+
+    def get_updated_skfs(self):
+        """Per-pair dicts of live parameters (the data ``Skf.from_dict`` would wrap)."""
+        out = {}
+        for key, opt in self.skf_optimizers.items():
+            d = dict(opt.skf_dict)
+            d["hamiltonian"] = dict(opt.h_params.items())
+            d["overlap"] = dict(opt.s_params.items())
+            out[key] = d
+        return out
+
+    def apply_constraints(self):
+        for opt in self.skf_optimizers.values():
+            opt.apply_constraints()
+
+    # ------------------------------------------------------------- feeding
+    def _param_signature(self, device):
+        sig = [str(device)]
+        for key, opt in self.skf_optimizers.items():
+            for p in list(opt.h_params.values()) + list(opt.s_params.values()):
+                sig.append((id(p), p._version, p.data_ptr()))
+        return tuple(sig)
+
+    def table_set(self, shell_dict: Dict[int, List[int]], device, species: Optional[Sequence[int]] = None):
+        """Packed device tables for ``species`` (all elements of the model by default), cached."""
+        species = sorted(set(int(z) for z in (species if species is not None else self._elements())))
+        key = (self._param_signature(device), tuple(species),
+               tuple((z, tuple(shell_dict[z])) for z in species))
+        if self._table_cache is not None and self._table_cache[0] == key:
+            return self._table_cache[1]
+        h, s, steps, onsite, occ = {}, {}, {}, {}, {}
+        sset = set(species)
+        for key_, opt in self.skf_optimizers.items():
+            za, zb = opt.atom_pair
+            if za not in sset or zb not in sset:
+                continue
+            h[(za, zb)] = {tuple(int(x) for x in k.split("-")): v for k, v in opt.h_params.items()}
+            s[(za, zb)] = {tuple(int(x) for x in k.split("-")): v for k, v in opt.s_params.items()}
+            steps[(za, zb)] = opt.grid_step
+            if za == zb and opt.atomic_data is not None:
+                onsite[za] = np.asarray(opt.atomic_data["on_sites"], dtype=np.float64)
+                occ[za] = np.asarray(opt.atomic_data["occupations"], dtype=np.float64)
+        missing = [z for z in species if z not in onsite]
+        if missing:
+            raise ValueError(f"no homonuclear parameters (on-site energies) for Z={missing}")
+        ts = E.TableSet(species, shell_dict, h, s, steps, onsite, occ, device)
+        self._table_cache = (key, ts)
+        return ts
+
+    def _elements(self):
+        zs = set()
+        for opt in self.skf_optimizers.values():
+            zs.update(opt.atom_pair)
+        return zs
+
+    # ----------------------------------------------------------- properties
+    def compute_properties_batch(self, structures: Sequence[dict], shell_dict=None, device=None,
+                                 dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
+                                 dos_window: float = 0.0, cutoff: float = E.CUTOFF_BOHR, engine=None):
+        """Batched path: many structures (each with its own k-points) in one launch sequence.
+
+        Each structure is a dict with ``numbers``, ``positions`` and ``cell``
+        (Bohr) and ``kpoints`` ([nk, 3] fractional; optional ``weights``).
+        Returns the ``BatchResult`` (device tensors).
+        """
+        device = torch.device(device if device is not None else "cuda")
+        shell_dict = shell_dict if shell_dict is not None else _default_shell_dict()
+        zs = sorted(set(int(z) for st in structures for z in np.asarray(st["numbers"]).reshape(-1)))
+        ts = self.table_set(shell_dict, device, zs)
+        eng = engine or E.Engine(ts, cutoff)
+        plan = E.plan_batch(structures, ts, cutoff)
+        res = eng.run(plan, dos_range, dos_points, dos_sigma, dos_window)
+        eng.check_tables()
+        return res
+
+    def compute_multi_element_properties(self, geometry=None, shell_dict=None, kpoints=None, klines=None,
+                                         phonons=False, get_fermi=False, get_energy=False, get_forces=False,
+                                         get_bulk_mod=False, device=None, with_eigenvectors=False):
+        """Reference signature (slakonet/optim.py:949-962); returns ``(properties, True)``."""
+        if phonons or get_energy or get_forces or get_bulk_mod:
+            raise NotImplementedError("phonons, total energy, forces and bulk modulus are outside this path")
+        if with_eigenvectors:
+            raise NotImplementedError("eigenvectors are not produced by this path yet")
+        if device is None:
+            device = "cuda"
+        device = torch.device(device)
+        shell_dict = shell_dict if shell_dict is not None else _default_shell_dict()
+        st = _structure_from_geometry(geometry)
+        if klines is not None:
+            k = klines_kpoints(klines)
+        elif kpoints is not None:
+            k = mp_kpoints(torch.as_tensor(kpoints).detach().cpu().numpy())
+        else:
+            k = mp_kpoints([1, 1, 1])
+        st["kpoints"] = k
+        st["weights"] = np.full(len(k), 1.0 / len(k))
+        res = self.compute_properties_batch([st], shell_dict, device)
+        return properties_dict(res, 0, get_fermi=get_fermi), True
+
+
+def _default_shell_dict():
+    from .synthetic import default_shell_dict
+    return default_shell_dict()
+
+
+def properties_dict(res: "E.BatchResult", s: int, get_fermi: bool = False) -> dict:
+    """The reference's properties dict for structure ``s`` of a batch result."""
+    plan = res.plan
+    st = res.stats[s].detach().cpu().numpy()
+    I = E.STAT
+    dev = res.eig.device
+    eig = res.eigenvalues(s).unsqueeze(0)
+    metal_or_fallback = st[I["metal"]] > 0 or st[I["fallback"]] > 0
+    gap_t = torch.tensor(float(st[I["gap_ev"]]), dtype=torch.float64, device="cpu" if metal_or_fallback else dev)
+    mdg = st[I["min_dgap"]]
+    dos = res.dos[s]
+    props = {
+        "fermi_energy_eV": float(st[I["fermi_ev"]]),
+        "fermi_energy_Ha": float(st[I["mu_ha"]]),
+        "band_gap_eV": gap_t,
+        "vbm_eV": float(st[I["vbm_ev"]]),
+        "cbm_eV": float(st[I["cbm_ev"]]),
+        "is_direct_gap": bool(st[I["direct"]] > 0),
+        "vbm_kpoint": int(st[I["vbm_k"]]),
+        "cbm_kpoint": int(st[I["cbm_k"]]),
+        "valence_band_width_eV": float(st[I["vwidth"]]),
+        "conduction_band_width_eV": float(st[I["cwidth"]]),
+        "minimum_direct_gap_eV": None if np.isnan(mdg) else float(mdg),
+        "is_direct_semiconductor": torch.tensor(bool(st[I["direct_semi"]] > 0)),
+        "nkpoints": int(plan.nk[s]),
+        "nbands": int(plan.nb[s]),
+        "nelectrons": int(plan.nelec[s]),
+        "dos_at_fermi": float(st[I["dos_fermi"]]),
+        "dos_gap_center_eV": float(st[I["dos_gapc"]]),
+        "dos_total_states": float(st[I["dos_total"]]),
+        "dos_at_fermi_tensor": res.stats[s, I["dos_fermi"]],
+        "dos_gap_center_tensor": res.stats[s, I["dos_gapc"]],
+        "dos_total_states_tensor": res.stats[s, I["dos_total"]],
+        "dos_energy_grid_tensor": res.dos_grid,
+        "dos_values_tensor": dos,
+        "fermi_converged": bool(st[I["converged"]] > 0),
+    }
+    k0 = int(plan.k_ptr[s])
+    nk = int(plan.nk[s])
+    calc = types.SimpleNamespace(
+        eigenvalue=eig,
+        k_weights=torch.as_tensor(plan.kweights[k0:k0 + nk]).unsqueeze(0),
+        kpoints=torch.as_tensor(plan.kpoints[k0:k0 + nk]).unsqueeze(0),
+        nelectron=torch.tensor([plan.nelec[s]]),
+        eig_status=res.eig_status[plan.prob_struct == s] if False else None,
+    )
+    if get_fermi:
+        props["efermi"] = (res.mu[s] * H2E).reshape(1, 1, 1)
+        props["bandgap"] = res.stats[s, I["bandgap_ev"]].reshape(1)
+        props["calc"] = calc
+    props["eigenvalues"] = eig
+    return props

@@ -28,5 +28,7 @@ def load_case(g):
         sd = syn.default_shell_dict()
         tables = syn.make_tables(st["numbers"], sd, seed=int(g["table_seed"]))
         sd = {int(z): sd[int(z)] for z in st["numbers"]}
-    np.testing.assert_allclose(tables_checksum(tables), g["tables_checksum"], rtol=0, atol=0)
+    # numpy's exp differs by an ulp between x86 and aarch64 builds, so the regenerated
+    # tables match the fixture's to rounding, not bit for bit
+    np.testing.assert_allclose(tables_checksum(tables), g["tables_checksum"], rtol=1e-12, atol=1e-300)
     return st, tables, sd

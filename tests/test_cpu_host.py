@@ -1,0 +1,124 @@
+"""Host-side logic and the C ABI library, without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+from oracle import slako_oracle as O
+from slakonet_gb300 import _lib, engine as E, model as M, synthetic as syn
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "slakonet_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^int\s+(skn_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = header_functions()
+    assert len(names) >= 9
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _lib.SIGNATURES, n
+    assert lib.skn_abi_version() == 100
+
+
+def test_argument_errors_without_gpu():
+    # invalid arguments are rejected before any launch
+    assert _lib.load().skn_eigh_gen_batched(-1, None, None, None, None, None, None, None, None, None, 0, None) == 1
+    assert _lib.load().skn_dos(1, None, None, None, None, None, None, None, 0.0, 1.0, 0, 0.1, 0.0,
+                               None, None, None, None) == 1
+
+
+def _walk_bonds(plan, s, cutoff):
+    """numpy replica of the kernel's translation-box walk for structure s."""
+    a0, a1 = plan.atom_ptr[s], plan.atom_ptr[s + 1]
+    pos = plan.positions[a0:a1]
+    cell = plan.cells[s]
+    r = plan.image_range[s]
+    T = np.array([[i, j, k] for i in range(-r[0], r[0] + 1) for j in range(-r[1], r[1] + 1)
+                  for k in range(-r[2], r[2] + 1)], float)
+    v = pos[None, None, :, :] + (T @ cell)[:, None, None, :] - pos[None, :, None, :]
+    d = np.sqrt((v * v).sum(-1))
+    c, i, j = np.nonzero((d < cutoff) & (d > 0))
+    return set(zip(i.tolist(), j.tolist(), map(tuple, T[c].astype(int).tolist())))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_image_range_covers_every_bond(seed):
+    rng = np.random.default_rng(seed)
+    sts = []
+    for n in (2, 5, 11):
+        st = syn.random_structure(rng, n, zmax=30)
+        st["kpoints"] = np.zeros((1, 3))
+        sts.append(st)
+    sts.append(dict(syn.diamond_si(), kpoints=np.zeros((1, 3))))
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    tables = syn.make_tables(zs, syn.default_shell_dict(), seed=seed)
+    ts = E.TableSet.from_synthetic(tables, syn.default_shell_dict(), "cpu")
+    plan = E.plan_batch(sts, ts)
+    for s, st in enumerate(sts):
+        i, j, T, d, u = O.bond_list(st["positions"], st["cell"], 10.0, rcut_images=30.0)
+        ref = set(zip(i.tolist(), j.tolist(), map(tuple, T.tolist())))
+        assert _walk_bonds(plan, s, 10.0) == ref
+
+
+def test_plan_offsets_are_consistent():
+    rng = np.random.default_rng(4)
+    sts = []
+    for n in (3, 7, 2):
+        st = syn.random_structure(rng, n)
+        st["kpoints"] = syn.gamma_centred_kpoints(syn.gamma_centred_grid(st["cell"], n, 50))
+        sts.append(st)
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    ts = E.TableSet.from_synthetic(syn.make_tables(zs, syn.default_shell_dict(), seed=1), syn.default_shell_dict(), "cpu")
+    p = E.plan_batch(sts, ts)
+    assert p.hs_total == int(sum(int(p.nb[s]) ** 2 * int(p.nk[s]) for s in range(p.n_struct)))
+    ends = p.hs_off + p.prob_n.astype(np.int64) ** 2
+    assert ends.max() == p.hs_total and (p.hs_off[1:] == ends[:-1]).all()
+    assert (p.eig_off_prob + p.prob_n <= p.eig_total).all()
+    assert sorted(p.order.tolist()) == list(range(len(p.prob_n)))
+    assert (np.diff(p.prob_n[p.order]) <= 0).all()
+    nimg = np.prod(2 * p.image_range + 1, axis=1)
+    assert p.n_phase == int((nimg * p.nk).sum())
+
+
+def test_kpoint_generators_match_reference():
+    g = golden("si_cfg0")
+    np.testing.assert_array_equal(M.mp_kpoints([8, 8, 8]), g["kpoints"])
+    g = golden("si_klines")
+    assert np.abs(M.klines_kpoints(g["klines"]) - g["kpoints"]).max() <= 1e-15
+
+
+def test_state_dict_layout_matches_reference_keys():
+    tables = syn.make_tables([6, 14], syn.default_shell_dict(), seed=0)
+    m = M.MultiElementSkfParameterOptimizer.from_tables(tables)
+    keys = set(m.state_dict().keys())
+    assert "skf_optimizers.Si-C.h_params.0-1" in keys
+    assert "skf_optimizers.C-C.s_params.1-1" in keys
+    p = m.skf_optimizers["Si-Si"].h_params["1-1"]
+    assert p.dtype.is_floating_point and p.shape == (2, len(tables["grid"]))
+
+
+def test_apply_constraints_clamps_to_band():
+    tables = syn.make_tables([14], {14: [0, 1]}, seed=0)
+    m = M.MultiElementSkfParameterOptimizer.from_tables(tables)
+    p = m.skf_optimizers["Si-Si"].h_params["0-1"]
+    o = p.detach().clone()
+    with __import__("torch").no_grad():
+        p.mul_(3.0)
+    m.apply_constraints()
+    lo = np.minimum(o * 0.7, o * 1.3)
+    hi = np.maximum(o * 0.7, o * 1.3)
+    v = p.detach().numpy()
+    assert (v >= lo.numpy() - 1e-15).all() and (v <= hi.numpy() + 1e-15).all()
+
+
+def test_engine_refuses_cpu():
+    ts = E.TableSet.from_synthetic(syn.make_tables([1], {1: [0]}, seed=0), {1: [0]}, "cpu")
+    with pytest.raises(_lib.SknError):
+        E.Engine(ts)
