@@ -22,14 +22,28 @@
 
 namespace {
 
-constexpr int NT = 256;           // threads per CTA
+// Launch shape knobs (compile-time; tuned by the size sweep):
+#ifndef SKN_EIG_NT
+#define SKN_EIG_NT 256
+#endif
+#ifndef SKN_EIG_MINB
+#define SKN_EIG_MINB 3
+#endif
+#ifndef SKN_EIG_UNR
+#define SKN_EIG_UNR 2
+#endif
+#ifndef SKN_EIG_SMEM_N
+#define SKN_EIG_SMEM_N 32
+#endif
+constexpr int NT = SKN_EIG_NT;    // threads per CTA
 constexpr int NW = NT / 32;
-constexpr int SMEM_N = 40;        // problems up to this size run from shared memory
+constexpr int SMEM_N = SKN_EIG_SMEM_N;   // problems up to this size run from shared memory
 constexpr int SMEM_LDA = SMEM_N + 1;
 constexpr int MAX_N = 2048;       // shared-memory vectors bound the single-CTA path
 
 struct Vecs {
-  double2* w;      // n: hemv result / Householder w
+  double2* v;      // n: working column / Householder vector
+  double2* w;      // n: hemv result / Householder w / L column
   double* d;       // n: tridiagonal diagonal
   double* e2;      // n: squared off-diagonal (e2[i] couples i and i+1)
   double* rdiag;   // n: 1 / L[i][i]
@@ -39,19 +53,13 @@ struct Vecs {
   float* e232;     // n: FP32 copy of e^2
 };
 
-__device__ __forceinline__ double2 ld(const double2* A, int lda, int i, int j) { return A[i + (int64_t)j * lda]; }
-__device__ __forceinline__ void st(double2* A, int lda, int i, int j, double2 v) { A[i + (int64_t)j * lda] = v; }
-
-// Hermitian A (lower stored), rows >= r0: returns conj-aware element (i, j) of the full matrix.
-__device__ __forceinline__ double2 herm(const double2* A, int lda, int i, int j) {
-  const bool up = j > i;
-  double2 v = up ? A[j + (int64_t)i * lda] : A[i + (int64_t)j * lda];
-  v.y = cond_flip(v.y, up);
-  return v;
-}
-
 // ---------------------------------------------------------------- Cholesky
-__device__ bool cholesky_lower(double2* A, int lda, int n, Vecs& V) {
+// Loops over the trailing triangle issue UNR independent loads per thread
+// before their FMAs: with FP64 this slow, the kernel is bound by how many
+// global loads each SM keeps in flight, not by bandwidth.
+constexpr int UNR = SKN_EIG_UNR;
+
+__device__ bool cholesky_lower(double2* __restrict__ A, int lda, int n, Vecs& V) {
   const int tid = threadIdx.x;
   for (int k = 0; k < n; ++k) {
     if (tid == 0) {
@@ -68,89 +76,136 @@ __device__ bool cholesky_lower(double2* A, int lda, int n, Vecs& V) {
     if (reinterpret_cast<int*>(V.sc)[2]) return false;
     const double rd = V.sc[0];
     const int m = n - k - 1;
+    double2* col = A + (k + 1) + (int64_t)k * lda;
     for (int i = tid; i < m; i += NT) {
-      double2 v = A[(k + 1 + i) + (int64_t)k * lda];
-      A[(k + 1 + i) + (int64_t)k * lda] = cscale(v, rd);
+      const double2 v = cscale(col[i], rd);
+      col[i] = v;
+      V.v[i] = v;
     }
     __syncthreads();
-    // trailing update of the packed lower triangle (k < j <= i)
+    // trailing update of the packed lower triangle (k < j <= i): A_ij -= l_i conj(l_j)
     const int tri = m * (m + 1) / 2;
-    for (int e = tid; e < tri; e += NT) {
-      int ii, jj;
-      tri_index(e, m, ii, jj);
-      const int i = k + 1 + ii, j = k + 1 + jj;
-      const double2 aik = A[i + (int64_t)k * lda];
-      const double2 ajk = A[j + (int64_t)k * lda];
-      A[i + (int64_t)j * lda] = cfms_conj(aik, ajk, A[i + (int64_t)j * lda]);
+    double2* T = A + (k + 1) + (int64_t)(k + 1) * lda;
+    for (int e0 = tid; e0 < tri; e0 += NT * UNR) {
+      int off[UNR], ii[UNR], jj[UNR];
+      double2 a[UNR];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const int e = e0 + u * NT;
+        if (e < tri) {
+          tri_index(e, m, ii[u], jj[u]);
+          off[u] = ii[u] + jj[u] * lda;
+          a[u] = T[off[u]];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        if (e0 + u * NT < tri) T[off[u]] = cfms_conj(V.v[ii[u]], V.v[jj[u]], a[u]);
+      }
     }
     __syncthreads();
   }
   return true;
 }
 
-// y[i] = sum_j Herm(A)[r0+i][r0+j] x[j] for i < m, x and y in shared/global memory.
-// Rows on lanes with a uniform trip count over j; when fewer than NT rows,
-// warps split the j range and partial sums are added through `y` + red.
-__device__ void hemv_lower(const double2* A, int lda, int r0, int m, const double2* x, double2* y, double2 scale,
-                           double* red_c /* 2*NT doubles of scratch */) {
+// y[i] = scale * sum_j Herm(A22)[i][j] x[j] for i < m, A22 at A (lower stored),
+// x in shared memory.  Rows on lanes with a uniform trip count over j, UNR
+// loads in flight per thread; with fewer rows than threads, warps split the
+// j range and partial sums are combined through `part`.
+__device__ void hemv_lower(const double2* __restrict__ A, int lda, int m, const double2* __restrict__ x,
+                           double2* __restrict__ y, double2 scale, double2* __restrict__ part) {
   const int tid = threadIdx.x;
   const int row_warps = (m + 31) >> 5;
-  if (row_warps >= NW) {
-    for (int i = tid; i < m; i += NT) {
-      double2 acc = make_double2(0.0, 0.0);
-      const int gi = r0 + i;
-      for (int j = 0; j < m; ++j) acc = cfma(herm(A, lda, gi, r0 + j), x[j], acc);
-      y[i] = cmul(scale, acc);
-    }
-    __syncthreads();
-    return;
-  }
-  const int nsplit = NW / row_warps;
+  const int nsplit = row_warps >= NW ? 1 : NW / row_warps;
   const int w = tid >> 5, lane = tid & 31;
-  const int rb = w % row_warps, sp = w / row_warps;
-  const int i = rb * 32 + lane;
-  double2 acc = make_double2(0.0, 0.0);
-  if (sp < nsplit) {
-    const int chunk = (m + nsplit - 1) / nsplit;
-    const int j0 = sp * chunk, j1 = min(m, j0 + chunk);
-    const int gi = r0 + min(i, m - 1);
-    for (int j = j0; j < j1; ++j) acc = cfma(herm(A, lda, gi, r0 + j), x[j], acc);
-  }
-  double2* part = reinterpret_cast<double2*>(red_c);
-  part[tid] = acc;
-  __syncthreads();
-  for (int r = tid; r < m; r += NT) {
-    double2 s = make_double2(0.0, 0.0);
-    const int rbw = r >> 5, ln = r & 31;
-    for (int q = 0; q < nsplit; ++q) {
-      const double2 v = part[(q * row_warps + rbw) * 32 + ln];
-      s.x += v.x;
-      s.y += v.y;
+  const int rows_per_pass = (nsplit == 1) ? NT : row_warps * 32;
+  const int sp = (nsplit == 1) ? 0 : w / row_warps;
+  const int r_in = (nsplit == 1) ? tid : (w % row_warps) * 32 + lane;
+  const int chunk = (m + nsplit - 1) / nsplit;
+  const int j0 = sp * chunk, j1 = min(m, j0 + chunk);
+  for (int rbase = 0; rbase < m; rbase += rows_per_pass) {
+    const int i = min(rbase + r_in, m - 1);
+    double2 acc0 = make_double2(0.0, 0.0), acc1 = make_double2(0.0, 0.0);
+    if (sp < nsplit) {
+      int j = j0;
+      for (; j + UNR <= j1; j += UNR) {
+        double2 a[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+          const int jj = j + u;
+          const bool up = jj > i;
+          a[u] = up ? A[jj + (int64_t)i * lda] : A[i + (int64_t)jj * lda];
+          a[u].y = cond_flip(a[u].y, up);
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; u += 2) {
+          acc0 = cfma(a[u], x[j + u], acc0);
+          acc1 = cfma(a[u + 1], x[j + u + 1], acc1);
+        }
+      }
+      for (; j < j1; ++j) {
+        const bool up = j > i;
+        double2 a = up ? A[j + (int64_t)i * lda] : A[i + (int64_t)j * lda];
+        a.y = cond_flip(a.y, up);
+        acc0 = cfma(a, x[j], acc0);
+      }
     }
-    y[r] = cmul(scale, s);
+    acc0.x += acc1.x;
+    acc0.y += acc1.y;
+    if (nsplit == 1) {
+      if (rbase + r_in < m) y[rbase + r_in] = cmul(scale, acc0);
+    } else {
+      part[tid] = acc0;
+    }
+  }
+  if (nsplit > 1) {
+    __syncthreads();
+    for (int r = tid; r < m; r += NT) {
+      double2 s = make_double2(0.0, 0.0);
+      const int rbw = r >> 5, ln = r & 31;
+      for (int q = 0; q < nsplit; ++q) {
+        const double2 v = part[(q * row_warps + rbw) * 32 + ln];
+        s.x += v.x;
+        s.y += v.y;
+      }
+      y[r] = cmul(scale, s);
+    }
   }
   __syncthreads();
 }
 
-// A22 -= x y^H + y x^H on the packed lower triangle of rows/cols r0..r0+m-1.
-__device__ void her2_lower(double2* A, int lda, int r0, int m, const double2* x, int xinc_lda_col,
-                           const double2* y) {
-  (void)xinc_lda_col;
+// A22 -= x y^H + y x^H on the packed lower triangle (A22 at T), x and y in shared memory.
+__device__ void her2_lower(double2* __restrict__ T, int lda, int m, const double2* __restrict__ x,
+                           const double2* __restrict__ y) {
   const int tri = m * (m + 1) / 2;
-  for (int e = threadIdx.x; e < tri; e += NT) {
-    int ii, jj;
-    tri_index(e, m, ii, jj);
-    const int i = r0 + ii, j = r0 + jj;
-    double2 a = A[i + (int64_t)j * lda];
-    a = cfms_conj(x[ii], y[jj], a);
-    a = cfms_conj(y[ii], x[jj], a);
-    A[i + (int64_t)j * lda] = a;
+  for (int e0 = threadIdx.x; e0 < tri; e0 += NT * UNR) {
+    int off[UNR], ii[UNR], jj[UNR];
+    double2 a[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int e = e0 + u * NT;
+      if (e < tri) {
+        tri_index(e, m, ii[u], jj[u]);
+        off[u] = ii[u] + jj[u] * lda;
+        a[u] = T[off[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      if (e0 + u * NT < tri) {
+        double2 v = cfms_conj(x[ii[u]], y[jj[u]], a[u]);
+        T[off[u]] = cfms_conj(y[ii[u]], x[jj[u]], v);
+      }
+    }
   }
 }
 
 // ------------------------------------------------- reduction to standard form
-// A (lower) <- L^-1 A L^-H with B = L from cholesky_lower (rdiag holds 1/L_kk).
-__device__ void hegs2_lower(double2* A, int lda, const double2* B, int ldb, int n, Vecs& V) {
+// A (lower) <- L^-1 A L^-H with B = L from cholesky_lower (rdiag holds 1/L_kk),
+// column by column in LAPACK zhegs2 order.  The working column and the L
+// column live in shared memory for the rank-2 update and the solve.
+__device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __restrict__ B, int ldb, int n,
+                            Vecs& V, double2* tile) {
   const int tid = threadIdx.x;
   for (int k = 0; k < n; ++k) {
     if (tid == 0) {
@@ -164,17 +219,21 @@ __device__ void hegs2_lower(double2* A, int lda, const double2* B, int ldb, int 
     if (m == 0) break;
     const double ct = V.sc[0];
     const double rd = V.rdiag[k];
-    double2* a = A + (k + 1) + (int64_t)k * lda;       // column k below the diagonal
-    const double2* b = B + (k + 1) + (int64_t)k * ldb;
+    double2* acol = A + (k + 1) + (int64_t)k * lda;
+    const double2* bcol = B + (k + 1) + (int64_t)k * ldb;
+    double2* a = V.v;
+    double2* b = V.w;
     for (int i = tid; i < m; i += NT) {
-      double2 v = cscale(a[i], rd);
-      v.x = fma(ct, b[i].x, v.x);
-      v.y = fma(ct, b[i].y, v.y);
+      const double2 bi = bcol[i];
+      double2 v = cscale(acol[i], rd);
+      v.x = fma(ct, bi.x, v.x);
+      v.y = fma(ct, bi.y, v.y);
       a[i] = v;
+      b[i] = bi;
     }
     __syncthreads();
-    her2_lower(A, lda, k + 1, m, a, 0, b);
-    __syncthreads();
+    her2_lower(A + (k + 1) + (int64_t)(k + 1) * lda, lda, m, a, b);
+    __syncthreads();   // the update above reads a[]; the axpy below rewrites it
     for (int i = tid; i < m; i += NT) {
       double2 v = a[i];
       v.x = fma(ct, b[i].x, v.x);
@@ -182,58 +241,95 @@ __device__ void hegs2_lower(double2* A, int lda, const double2* B, int ldb, int 
       a[i] = v;
     }
     __syncthreads();
-    // forward substitution a <- L22^-1 a, in chunks of 32 rows: warp 0 solves the
+    // forward substitution a <- L22^-1 a in chunks of 32 rows: warp 0 solves the
     // diagonal chunk, then all threads apply it to the rows below.
+    const double2* L = B + (k + 1) + (int64_t)(k + 1) * ldb;
     for (int c0 = 0; c0 < m; c0 += 32) {
       const int cm = min(32, m - c0);
+      // stage the cm x cm diagonal block of L (from global memory) in the tile
+      const double2* Ld = L + c0 + (int64_t)c0 * ldb;
+      int ldt = ldb;
+      if (tile != nullptr) {
+        for (int e = tid; e < cm * 32; e += NT) {
+          const int r = e & 31, c = e >> 5;
+          if (r < cm) tile[r + c * 33] = Ld[r + (int64_t)c * ldb];
+        }
+        __syncthreads();
+        Ld = tile;
+        ldt = 33;
+      }
       if (tid < 32) {
         const int lane = tid;
-        double2 x = (lane < cm) ? a[c0 + lane] : make_double2(0.0, 0.0);
+        double2 xv = (lane < cm) ? a[c0 + lane] : make_double2(0.0, 0.0);
         for (int i = 0; i < cm; ++i) {
+          if (lane == i) xv = cscale(xv, V.rdiag[k + 1 + c0 + i]);
           double2 xi;
-          if (lane == i) {
-            x = cscale(x, V.rdiag[k + 1 + c0 + i]);
-          }
-          xi.x = __shfl_sync(0xffffffffu, x.x, i);
-          xi.y = __shfl_sync(0xffffffffu, x.y, i);
+          xi.x = __shfl_sync(0xffffffffu, xv.x, i);
+          xi.y = __shfl_sync(0xffffffffu, xv.y, i);
           if (lane > i && lane < cm) {
-            const double2 l = B[(k + 1 + c0 + lane) + (int64_t)(k + 1 + c0 + i) * ldb];
-            x.x = fma(-xi.x, l.x, x.x);
-            x.x = fma(xi.y, l.y, x.x);
-            x.y = fma(-xi.x, l.y, x.y);
-            x.y = fma(-xi.y, l.x, x.y);
+            const double2 l = Ld[lane + (int64_t)i * ldt];
+            xv.x = fma(-xi.x, l.x, xv.x);
+            xv.x = fma(xi.y, l.y, xv.x);
+            xv.y = fma(-xi.x, l.y, xv.y);
+            xv.y = fma(-xi.y, l.x, xv.y);
           }
         }
-        if (lane < cm) a[c0 + lane] = x;
+        if (lane < cm) a[c0 + lane] = xv;
       }
       __syncthreads();
       const int rest = m - c0 - cm;
       for (int r = tid; r < rest; r += NT) {
         const int row = c0 + cm + r;
-        double2 v = a[row];
-        for (int i = 0; i < cm; ++i) {
-          const double2 xi = a[c0 + i];
-          const double2 l = B[(k + 1 + row) + (int64_t)(k + 1 + c0 + i) * ldb];
-          v.x = fma(-xi.x, l.x, v.x);
-          v.x = fma(xi.y, l.y, v.x);
-          v.y = fma(-xi.x, l.y, v.y);
-          v.y = fma(-xi.y, l.x, v.y);
+        double2 v0 = a[row], v1 = make_double2(0.0, 0.0);
+        const double2* Lr = L + row + (int64_t)c0 * ldb;
+        int i = 0;
+        for (; i + UNR <= cm; i += UNR) {
+          double2 l[UNR];
+#pragma unroll
+          for (int u = 0; u < UNR; ++u) l[u] = Lr[(int64_t)(i + u) * ldb];
+#pragma unroll
+          for (int u = 0; u < UNR; u += 2) {
+            const double2 x0 = a[c0 + i + u], x1 = a[c0 + i + u + 1];
+            v0.x = fma(-x0.x, l[u].x, v0.x);
+            v0.x = fma(x0.y, l[u].y, v0.x);
+            v0.y = fma(-x0.x, l[u].y, v0.y);
+            v0.y = fma(-x0.y, l[u].x, v0.y);
+            v1.x = fma(-x1.x, l[u + 1].x, v1.x);
+            v1.x = fma(x1.y, l[u + 1].y, v1.x);
+            v1.y = fma(-x1.x, l[u + 1].y, v1.y);
+            v1.y = fma(-x1.y, l[u + 1].x, v1.y);
+          }
         }
-        a[row] = v;
+        for (; i < cm; ++i) {
+          const double2 x0 = a[c0 + i], l0 = Lr[(int64_t)i * ldb];
+          v0.x = fma(-x0.x, l0.x, v0.x);
+          v0.x = fma(x0.y, l0.y, v0.x);
+          v0.y = fma(-x0.x, l0.y, v0.y);
+          v0.y = fma(-x0.y, l0.x, v0.y);
+        }
+        a[row] = make_double2(v0.x + v1.x, v0.y + v1.y);
       }
       __syncthreads();
     }
+    for (int i = tid; i < m; i += NT) acol[i] = a[i];
+    __syncthreads();
   }
 }
 
 // ------------------------------------------------------ tridiagonalisation
-__device__ void hetd2_lower(double2* A, int lda, int n, Vecs& V) {
+// LAPACK zhetd2 (lower): reflector from column k, w = tau A22 v,
+// w -= (tau/2)(w^H v) v, A22 -= v w^H + w v^H.  d and e^2 go to shared memory.
+__device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V) {
   const int tid = threadIdx.x;
   for (int k = 0; k < n - 1; ++k) {
     const int m = n - k - 1;
     double2* x = A + (k + 1) + (int64_t)k * lda;
     double s = 0.0;
-    for (int i = 1 + tid; i < m; i += NT) s = fma(x[i].x, x[i].x, fma(x[i].y, x[i].y, s));
+    for (int i = 1 + tid; i < m; i += NT) {
+      const double2 xi = x[i];
+      V.v[i] = xi;
+      s = fma(xi.x, xi.x, fma(xi.y, xi.y, s));
+    }
     const double xnorm2 = block_sum(s, V.red);
     if (tid == 0) {
       const double2 alpha = x[0];
@@ -263,36 +359,37 @@ __device__ void hetd2_lower(double2* A, int lda, int n, Vecs& V) {
       reinterpret_cast<int*>(V.sc)[10] = trivial;
       V.d[k] = A[k + (int64_t)k * lda].x;
       V.e2[k] = beta * beta;
+      V.v[0] = make_double2(1.0, 0.0);
     }
     __syncthreads();
     const int trivial = reinterpret_cast<int*>(V.sc)[10];
     const double2 tau = make_double2(V.sc[1], V.sc[2]);
     if (!trivial) {
       const double2 scl = make_double2(V.sc[3], V.sc[4]);
-      for (int i = 1 + tid; i < m; i += NT) x[i] = cmul(x[i], scl);
-      if (tid == 0) x[0] = make_double2(1.0, 0.0);
+      for (int i = 1 + tid; i < m; i += NT) {
+        const double2 v = cmul(V.v[i], scl);
+        V.v[i] = v;
+        x[i] = v;
+      }
       __syncthreads();
-      // w = tau * A22 v
-      hemv_lower(A, lda, k + 1, m, x, V.w, tau, V.red + 4 * NW);
-      // alpha2 = -1/2 tau (w^H v)
+      double2* T = A + (k + 1) + (int64_t)(k + 1) * lda;
+      hemv_lower(T, lda, m, V.v, V.w, tau, reinterpret_cast<double2*>(V.red + 4 * NW));
       double pr = 0.0, pi = 0.0;
       for (int i = tid; i < m; i += NT) {
-        const double2 wi = V.w[i], vi = x[i];
+        const double2 wi = V.w[i], vi = V.v[i];
         pr = fma(wi.x, vi.x, fma(wi.y, vi.y, pr));
         pi = fma(wi.x, vi.y, fma(-wi.y, vi.x, pi));
       }
       const double dre = block_sum(pr, V.red);
       const double dim = block_sum(pi, V.red + NW);
       const double2 al = cmul(make_double2(-0.5 * tau.x, -0.5 * tau.y), make_double2(dre, dim));
-      for (int i = tid; i < m; i += NT) V.w[i] = cfma(al, x[i], V.w[i]);
+      for (int i = tid; i < m; i += NT) V.w[i] = cfma(al, V.v[i], V.w[i]);
       __syncthreads();
-      her2_lower(A, lda, k + 1, m, x, 0, V.w);
+      her2_lower(T, lda, m, V.v, V.w);
       __syncthreads();
       if (tid == 0) x[0] = make_double2(V.sc[0], 0.0);
     } else {
-      if (tid == 0) {
-        A[(k + 1) + (int64_t)(k + 1) * lda].y = 0.0;
-      }
+      if (tid == 0) A[(k + 1) + (int64_t)(k + 1) * lda].y = 0.0;
     }
     __syncthreads();
   }
@@ -427,7 +524,7 @@ __device__ void aux_zero_rows(double2* A, int lda, int n) {
   }
 }
 
-__global__ void __launch_bounds__(NT) k_eigh_gen(int n_prob, const int32_t* __restrict__ nvec,
+__global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const int32_t* __restrict__ nvec,
                                                  const int64_t* __restrict__ hs_off,
                                                  const int64_t* __restrict__ eig_off,
                                                  const int32_t* __restrict__ order, double2* H, double2* S,
@@ -445,10 +542,11 @@ __global__ void __launch_bounds__(NT) k_eigh_gen(int n_prob, const int32_t* __re
     V.rdiag = p; p += max_n;
     p += (max_n & 1);
     V.w = reinterpret_cast<double2*>(p); p += 2 * max_n;
+    V.v = reinterpret_cast<double2*>(p); p += 2 * max_n;
     V.d32 = reinterpret_cast<float*>(V.rdiag);
     V.e232 = V.d32 + max_n;
   }
-  double2* Hs = reinterpret_cast<double2*>(smem + 16 + 4 * NW + 2 * NT + 3 * max_n + (max_n & 1) + 2 * max_n);
+  double2* Hs = reinterpret_cast<double2*>(smem + 16 + 4 * NW + 2 * NT + 3 * max_n + (max_n & 1) + 4 * max_n);
   double2* Ss = Hs + SMEM_LDA * SMEM_N;
   __shared__ int s_idx;
   for (;;) {
@@ -491,7 +589,7 @@ __global__ void __launch_bounds__(NT) k_eigh_gen(int n_prob, const int32_t* __re
       __syncthreads();
       continue;
     }
-    hegs2_lower(Ha, lda, Sa, lda, n, V);
+    hegs2_lower(Ha, lda, Sa, lda, n, V, in_smem ? nullptr : Hs);
     hetd2_lower(Ha, lda, n, V);
     if (n == 1 && tid == 0) V.d[0] = Ha[0].x;
     __syncthreads();
@@ -512,7 +610,7 @@ extern "C" int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t*
   if (max_n > MAX_N) return SKN_ERR_CAPACITY;
   const int mn = max_n < 1 ? 1 : max_n;
   const int use_smem_mats = 1;
-  size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 2 * (size_t)mn);
+  size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn);
   smem += (size_t)use_smem_mats * 2 * SMEM_LDA * SMEM_N * sizeof(double2);
   if (cudaFuncSetAttribute(k_eigh_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SKN_ERR_CUDA;
