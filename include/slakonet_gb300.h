@@ -151,6 +151,27 @@ int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t* hs_off, co
                          int32_t* work_counter, int max_n, cudaStream_t stream);
 
 /*
+ * Eigenvalues and eigenvectors of the same batched problems.  Replaces the
+ * eigenvector output of eighb (slakonet/utils.py:741-783) that
+ * SimpleDftb.__call__ keeps with with_eigenvectors (slakonet/main.py:137-196).
+ * Runs the values kernel keeping the reflectors, tau and the tridiagonal,
+ * then inverse iteration on the tridiagonal (clusters re-orthogonalised),
+ * the Householder back-transformation and x = L^-H y, so x^H S x = 1.
+ *   vec       out: complex, problem p at hs_off[p]; vec[i*n + j] = component i of eigenvector j
+ *   tri       scratch: 4 * sum(n) doubles (d, e, tau per problem at 4*eig_off[p])
+ *   scratch   scratch: skn_eigh_vectors_scratch_bytes(n_prob, max_n) bytes
+ *   work_counter  device int[2] scratch
+ * H and S are left holding the reflectors and L.
+ */
+int skn_eigh_gen_vectors(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                         const int32_t* order, double* H, double* S, double* eig, double* vec, int32_t* status,
+                         double* tri, double* scratch, int64_t scratch_bytes, int32_t* work_counter, int max_n,
+                         cudaStream_t stream);
+
+/* Host-side query: bytes of `scratch` skn_eigh_gen_vectors needs (written to *bytes). */
+int skn_eigh_vectors_scratch_bytes(int n_prob, int max_n, int64_t* bytes);
+
+/*
  * Fermi level, band gap and band-structure statistics per structure.
  * Replaces fermi_search / fermi_dirac (slakonet/fermi.py:139-215),
  * calculate_band_gap (slakonet/main.py:637-707),

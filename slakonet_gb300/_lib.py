@@ -42,6 +42,8 @@ SIGNATURES = {
     "skn_fermi_gap": [I32, P, P, P, P, P, P, P, F64, F64, I32, P, P, P, P],
     "skn_dos": [I32, P, P, P, P, P, P, P, F64, F64, I32, F64, F64, P, P, P, P],
     "skn_fp64_probe": [P, I32, I32, P],
+    "skn_eigh_gen_vectors": [I32, P, P, P, P, P, P, P, P, P, P, P, I64, P, I32, P],
+    "skn_eigh_vectors_scratch_bytes": [I32, I32, P],
 }
 
 

@@ -24,16 +24,16 @@ namespace {
 
 // Launch shape knobs (compile-time; tuned by the size sweep):
 #ifndef SKN_EIG_NT
-#define SKN_EIG_NT 256
+#define SKN_EIG_NT 128
 #endif
 #ifndef SKN_EIG_MINB
-#define SKN_EIG_MINB 3
+#define SKN_EIG_MINB 5
 #endif
 #ifndef SKN_EIG_UNR
 #define SKN_EIG_UNR 2
 #endif
 #ifndef SKN_EIG_SMEM_N
-#define SKN_EIG_SMEM_N 32
+#define SKN_EIG_SMEM_N 24
 #endif
 constexpr int NT = SKN_EIG_NT;    // threads per CTA
 constexpr int NW = NT / 32;
@@ -53,11 +53,21 @@ struct Vecs {
   float* e232;     // n: FP32 copy of e^2
 };
 
+// c - conj(a) * b
+__device__ __forceinline__ double2 cfms_conj_l(double2 a, double2 b, double2 c) {
+  c.x = fma(-a.x, b.x, c.x);
+  c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(-a.x, b.y, c.y);
+  c.y = fma(a.y, b.x, c.y);
+  return c;
+}
+
 // ---------------------------------------------------------------- Cholesky
 // Loops over the trailing triangle issue UNR independent loads per thread
 // before their FMAs: with FP64 this slow, the kernel is bound by how many
 // global loads each SM keeps in flight, not by bandwidth.
 constexpr int UNR = SKN_EIG_UNR;
+static_assert(UNR >= 2 && UNR % 2 == 0, "unrolled loops pair their accumulators");
 
 __device__ bool cholesky_lower(double2* __restrict__ A, int lda, int n, Vecs& V) {
   const int tid = threadIdx.x;
@@ -319,7 +329,7 @@ __device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __r
 // ------------------------------------------------------ tridiagonalisation
 // LAPACK zhetd2 (lower): reflector from column k, w = tau A22 v,
 // w -= (tau/2)(w^H v) v, A22 -= v w^H + w v^H.  d and e^2 go to shared memory.
-__device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V) {
+__device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V, double* tri) {
   const int tid = threadIdx.x;
   for (int k = 0; k < n - 1; ++k) {
     const int m = n - k - 1;
@@ -359,6 +369,11 @@ __device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V) {
       reinterpret_cast<int*>(V.sc)[10] = trivial;
       V.d[k] = A[k + (int64_t)k * lda].x;
       V.e2[k] = beta * beta;
+      if (tri != nullptr) {          // e (signed) and tau for the eigenvector back-transformation
+        tri[n + k] = beta;
+        tri[2 * n + 2 * k] = taur;
+        tri[2 * n + 2 * k + 1] = taui;
+      }
       V.v[0] = make_double2(1.0, 0.0);
     }
     __syncthreads();
@@ -395,6 +410,14 @@ __device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V) {
   }
   if (tid == 0) V.d[n - 1] = A[(n - 1) + (int64_t)(n - 1) * lda].x;
   __syncthreads();
+  if (tri != nullptr) {
+    for (int i = tid; i < n; i += NT) tri[i] = V.d[i];
+    if (tid == 0) {
+      tri[2 * n - 1] = 0.0;
+      tri[4 * n - 2] = 0.0;
+      tri[4 * n - 1] = 0.0;
+    }
+  }
 }
 
 // ------------------------------------------------------- Sturm bisection
@@ -529,7 +552,8 @@ __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const
                                                  const int64_t* __restrict__ eig_off,
                                                  const int32_t* __restrict__ order, double2* H, double2* S,
                                                  double* __restrict__ eig, int32_t* __restrict__ status,
-                                                 int32_t* __restrict__ counter, int max_n, int use_smem_mats) {
+                                                 int32_t* __restrict__ counter, int max_n, int use_smem_mats,
+                                                 double* __restrict__ tri_all) {
   extern __shared__ double smem[];
   const int tid = threadIdx.x;
   Vecs V;
@@ -590,15 +614,247 @@ __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const
       continue;
     }
     hegs2_lower(Ha, lda, Sa, lda, n, V, in_smem ? nullptr : Hs);
-    hetd2_lower(Ha, lda, n, V);
+    double* tri = tri_all != nullptr ? tri_all + 4 * eig_off[p] : nullptr;
+    hetd2_lower(Ha, lda, n, V, tri);
     if (n == 1 && tid == 0) V.d[0] = Ha[0].x;
     __syncthreads();
     tridiag_eigenvalues(n, V, eig + eig_off[p]);
+    if (tri != nullptr && in_smem) {   // reflectors and L must outlive the shared-memory stage
+      for (int e = tid; e < n * n; e += NT) {
+        const int i = e % n, j = e / n;
+        if (i >= j) {
+          Hg[e] = Ha[i + j * lda];
+          Sg[e] = Sa[i + j * lda];
+        }
+      }
+    }
     if (tid == 0) status[p] = SKN_OK;
     __syncthreads();
   }
 }
 
+
+// ============================================================= eigenvectors
+// Eigenvectors of H x = e S x for problems whose values kernel kept the
+// reflectors (lower triangle of H), tau, the tridiagonal (d, e) and L (in S):
+//   1. inverse iteration on T - e_j I (Gaussian elimination with partial
+//      pivoting on the tridiagonal, two solves from a pseudo-random start),
+//      one thread per eigenvalue; vectors of eigenvalues closer than 1e-9 of
+//      the spectrum's scale are re-orthogonalised (modified Gram-Schmidt, twice);
+//   2. y = Q z with Q = H_0 H_1 ... H_{n-2} (reflectors applied last first);
+//   3. x = L^-H y, so x^H S x = 1.
+// Vectors are written row-major per problem: vec[i*n + j] is component i of
+// eigenvector j (the reference's eigh column convention).
+constexpr int VNT = 128;
+constexpr int VNW = VNT / 32;
+
+__device__ __forceinline__ double hash_unit(unsigned a, unsigned b) {
+  unsigned h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u;
+  h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+  return (double)((int)(h & 0xFFFFFF) - 0x800000) * (1.0 / 8388608.0);   // [-1, 1)
+}
+
+__device__ double vblock_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int i = 0; i < VNW; ++i) t += red[i];
+  return t;
+}
+
+__global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __restrict__ nvec,
+                                                const int64_t* __restrict__ hs_off, const int64_t* __restrict__ eig_off,
+                                                const int32_t* __restrict__ order, const double2* __restrict__ H,
+                                                const double2* __restrict__ S, const double* __restrict__ eig,
+                                                const double* __restrict__ tri_all, const int32_t* __restrict__ status,
+                                                double2* __restrict__ vec, double* __restrict__ scratch,
+                                                int32_t* __restrict__ counter, int max_n) {
+  extern __shared__ double smem[];
+  double* red = smem;                                      // 2*VNW
+  double* d = smem + 2 * VNW;                              // max_n
+  double* e = d + max_n;                                   // max_n
+  double2* col = reinterpret_cast<double2*>(e + max_n);  // max_n (offset 2*VNW + 2*max_n doubles: even)
+  __shared__ int s_idx;
+  const int tid = threadIdx.x;
+  const int64_t sstride = (int64_t)max_n * VNT;
+  double* su = scratch + (int64_t)blockIdx.x * 5 * sstride;   // rows i: [i*VNT + tid]
+  double* s_ru1 = su;                 // 1 / u1
+  double* s_u2 = su + sstride;
+  double* s_u3 = su + 2 * sstride;
+  double* s_m = su + 3 * sstride;
+  double* s_pv = su + 4 * sstride;    // 1.0 where rows were swapped
+  for (;;) {
+    if (tid == 0) s_idx = atomicAdd(counter, 1);
+    __syncthreads();
+    const int idx = s_idx;
+    __syncthreads();
+    if (idx >= n_prob) break;
+    const int p = order[idx];
+    const int n = nvec[p];
+    double2* Y = vec + hs_off[p];
+    if (status[p] != SKN_OK) {
+      for (int q = tid; q < n * n; q += VNT) Y[q] = make_double2(__longlong_as_double(0x7ff8000000000000LL), 0.0);
+      __syncthreads();
+      continue;
+    }
+    const double* tri = tri_all + 4 * eig_off[p];
+    const double* w = eig + eig_off[p];
+    const double2* A = H + hs_off[p];
+    const double2* L = S + hs_off[p];
+    for (int i = tid; i < n; i += VNT) {
+      d[i] = tri[i];
+      e[i] = tri[n + i];
+    }
+    __syncthreads();
+    double scale = 0.0;
+    for (int i = tid; i < n; i += VNT) scale = fmax(scale, fabs(w[i]));
+    for (int o = 16; o > 0; o >>= 1) scale = fmax(scale, __shfl_xor_sync(0xffffffffu, scale, o));
+    __syncthreads();
+    if ((tid & 31) == 0) red[tid >> 5] = scale;
+    __syncthreads();
+    scale = red[0];
+    for (int q = 1; q < VNW; ++q) scale = fmax(scale, red[q]);
+    scale = fmax(scale, 1e-300);
+    const double pivmin = 1e-300 * fmax(1.0, scale);
+
+    // ---- 1. inverse iteration, one eigenvalue per thread
+    for (int j0 = 0; j0 < n; j0 += VNT) {
+      const int j = j0 + tid;
+      if (j < n) {
+        const double lam = w[j];
+        double u1 = d[0] - lam, u2 = (n > 1) ? e[0] : 0.0;
+        for (int i = 0; i < n - 1; ++i) {
+          const double c = e[i];
+          const double a1 = d[i + 1] - lam;
+          const double b1 = (i + 1 < n - 1) ? e[i + 1] : 0.0;
+          double m, r1, r2, r3, pv;
+          if (fabs(u1) >= fabs(c)) {
+            if (fabs(u1) < pivmin) u1 = (u1 < 0.0) ? -pivmin : pivmin;
+            m = c / u1;
+            r1 = u1; r2 = u2; r3 = 0.0; pv = 0.0;
+            u1 = a1 - m * u2;
+            u2 = b1;
+          } else {
+            m = u1 / c;
+            r1 = c; r2 = a1; r3 = b1; pv = 1.0;
+            u1 = u2 - m * a1;
+            u2 = -m * b1;
+          }
+          s_ru1[i * VNT + tid] = 1.0 / r1;
+          s_u2[i * VNT + tid] = r2;
+          s_u3[i * VNT + tid] = r3;
+          s_m[i * VNT + tid] = m;
+          s_pv[i * VNT + tid] = pv;
+        }
+        if (fabs(u1) < pivmin) u1 = (u1 < 0.0) ? -pivmin : pivmin;
+        s_ru1[(n - 1) * VNT + tid] = 1.0 / u1;
+        // y lives in the real parts of column j of Y
+        for (int i = 0; i < n; ++i) Y[(int64_t)i * n + j] = make_double2(hash_unit(j, i), 0.0);
+        for (int it = 0; it < 2; ++it) {
+          for (int i = 0; i < n - 1; ++i) {
+            const double m = s_m[i * VNT + tid];
+            const double yi = Y[(int64_t)i * n + j].x, yn = Y[(int64_t)(i + 1) * n + j].x;
+            if (s_pv[i * VNT + tid] != 0.0) {
+              Y[(int64_t)i * n + j].x = yn;
+              Y[(int64_t)(i + 1) * n + j].x = yi - m * yn;
+            } else {
+              Y[(int64_t)(i + 1) * n + j].x = yn - m * yi;
+            }
+          }
+          double x2 = 0.0, x1 = 0.0, nrm = 0.0;
+          for (int i = n - 1; i >= 0; --i) {
+            const double xi = (Y[(int64_t)i * n + j].x - s_u2[i * VNT + tid] * x1 - s_u3[i * VNT + tid] * x2) *
+                              s_ru1[i * VNT + tid];
+            Y[(int64_t)i * n + j].x = xi;
+            nrm = fma(xi, xi, nrm);
+            x2 = x1;
+            x1 = xi;
+          }
+          const double inv = 1.0 / sqrt(nrm);
+          for (int i = 0; i < n; ++i) Y[(int64_t)i * n + j].x *= inv;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- clusters: modified Gram-Schmidt (twice) within runs of close eigenvalues
+    {
+      const double ctol = 1e-9 * scale;
+      int j = 1;
+      while (j < n) {
+        if (w[j] - w[j - 1] > ctol) { ++j; continue; }
+        int j0 = j - 1, j1 = j + 1;
+        while (j1 < n && w[j1] - w[j1 - 1] <= ctol) ++j1;
+        for (int pass = 0; pass < 2; ++pass) {
+          for (int q = j0; q < j1; ++q) {
+            for (int r = j0; r < q; ++r) {
+              double dp = 0.0;
+              for (int i = tid; i < n; i += VNT) dp = fma(Y[(int64_t)i * n + r].x, Y[(int64_t)i * n + q].x, dp);
+              dp = vblock_sum(dp, red);
+              for (int i = tid; i < n; i += VNT) Y[(int64_t)i * n + q].x -= dp * Y[(int64_t)i * n + r].x;
+              __syncthreads();
+            }
+            double nn = 0.0;
+            for (int i = tid; i < n; i += VNT) nn = fma(Y[(int64_t)i * n + q].x, Y[(int64_t)i * n + q].x, nn);
+            nn = vblock_sum(nn, red);
+            const double inv = 1.0 / sqrt(nn);
+            for (int i = tid; i < n; i += VNT) Y[(int64_t)i * n + q].x *= inv;
+            __syncthreads();
+          }
+        }
+        j = j1;
+      }
+    }
+    __syncthreads();
+    // ---- 2. back-transformation y = Q z
+    for (int k = n - 2; k >= 0; --k) {
+      const double2 tau = make_double2(tri[2 * n + 2 * k], tri[2 * n + 2 * k + 1]);
+      if (tau.x == 0.0 && tau.y == 0.0) continue;
+      const int m = n - k - 1;
+      for (int r = tid; r < m; r += VNT)
+        col[r] = (r == 0) ? make_double2(1.0, 0.0) : A[(k + 1 + r) + (int64_t)k * n];
+      __syncthreads();
+      for (int jj = tid; jj < n; jj += VNT) {
+        double2 s0 = make_double2(0.0, 0.0), s1 = make_double2(0.0, 0.0);
+        int r = 0;
+        for (; r + 1 < m; r += 2) {
+          s0 = cfma_conj(col[r], Y[(int64_t)(k + 1 + r) * n + jj], s0);
+          s1 = cfma_conj(col[r + 1], Y[(int64_t)(k + 2 + r) * n + jj], s1);
+        }
+        if (r < m) s0 = cfma_conj(col[r], Y[(int64_t)(k + 1 + r) * n + jj], s0);
+        s0.x += s1.x;
+        s0.y += s1.y;
+        const double2 ts = cmul(tau, s0);          // y -= tau v (v^H y)
+        for (int q = 0; q < m; ++q) {
+          double2 y = Y[(int64_t)(k + 1 + q) * n + jj];
+          y = cfms_conj(col[q], make_double2(ts.x, -ts.y), y);
+          Y[(int64_t)(k + 1 + q) * n + jj] = y;
+        }
+      }
+      __syncthreads();
+    }
+    // ---- 3. x = L^-H y (backward substitution, one column per thread)
+    for (int i = n - 1; i >= 0; --i) {
+      const int m = n - i - 1;
+      for (int r = tid; r < m; r += VNT) col[r] = L[(i + 1 + r) + (int64_t)i * n];
+      if (tid == 0) col[max_n - 1] = L[i + (int64_t)i * n];
+      __syncthreads();
+      const double rl = 1.0 / col[max_n - 1].x;
+      for (int jj = tid; jj < n; jj += VNT) {
+        double2 acc0 = Y[(int64_t)i * n + jj], acc1 = make_double2(0.0, 0.0);
+        int r = 0;
+        for (; r + 1 < m; r += 2) {
+          acc0 = cfms_conj_l(col[r], Y[(int64_t)(i + 1 + r) * n + jj], acc0);
+          acc1 = cfms_conj_l(col[r + 1], Y[(int64_t)(i + 2 + r) * n + jj], acc1);
+        }
+        if (r < m) acc0 = cfms_conj_l(col[r], Y[(int64_t)(i + 1 + r) * n + jj], acc0);
+        Y[(int64_t)i * n + jj] = make_double2((acc0.x + acc1.x) * rl, (acc0.y + acc1.y) * rl);
+      }
+      __syncthreads();
+    }
+  }
+}
 }  // namespace
 
 extern "C" int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
@@ -623,6 +879,59 @@ extern "C" int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t*
   if (grid > n_prob) grid = n_prob;
   if (cudaMemsetAsync(work_counter, 0, sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
   k_eigh_gen<<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
-                                         work_counter, mn, use_smem_mats);
+                                         work_counter, mn, use_smem_mats, nullptr);
+  return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
+}
+
+static int vec_grid(int n_prob) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int g = 2 * (sms > 0 ? sms : 1);
+  return g < n_prob ? g : (n_prob > 0 ? n_prob : 1);
+}
+
+extern "C" int skn_eigh_vectors_scratch_bytes(int n_prob, int max_n, int64_t* bytes) {
+  if (!bytes || max_n < 0 || n_prob < 0) return SKN_ERR_ARG;
+  *bytes = (int64_t)vec_grid(n_prob) * 5 * (int64_t)(max_n < 1 ? 1 : max_n) * VNT * (int64_t)sizeof(double);
+  return SKN_OK;
+}
+
+extern "C" int skn_eigh_gen_vectors(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                                    const int32_t* order, double* H, double* S, double* eig, double* vec,
+                                    int32_t* status, double* tri, double* scratch, int64_t scratch_bytes,
+                                    int32_t* work_counter, int max_n, cudaStream_t stream) {
+  if (n_prob < 0 || max_n < 0) return SKN_ERR_ARG;
+  if (n_prob == 0) return SKN_OK;
+  if (!n || !hs_off || !eig_off || !order || !H || !S || !eig || !vec || !status || !tri || !scratch ||
+      !work_counter)
+    return SKN_ERR_ARG;
+  if (max_n > MAX_N) return SKN_ERR_CAPACITY;
+  int64_t need = 0;
+  skn_eigh_vectors_scratch_bytes(n_prob, max_n, &need);
+  if (scratch_bytes < need) return SKN_ERR_CAPACITY;
+  const int mn = max_n < 1 ? 1 : max_n;
+  const int use_smem_mats = 1;
+  size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn);
+  smem += (size_t)use_smem_mats * 2 * SMEM_LDA * SMEM_N * sizeof(double2);
+  if (cudaFuncSetAttribute(k_eigh_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return SKN_ERR_CUDA;
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigh_gen, NT, smem) != cudaSuccess || per_sm < 1)
+    return SKN_ERR_CUDA;
+  int grid = sms * per_sm;
+  if (grid > n_prob) grid = n_prob;
+  if (cudaMemsetAsync(work_counter, 0, 2 * sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
+  k_eigh_gen<<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
+                                         work_counter, mn, use_smem_mats, tri);
+  if (cudaPeekAtLastError() != cudaSuccess) return SKN_ERR_CUDA;
+  const size_t vsmem = sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;
+  if (cudaFuncSetAttribute(k_eigvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem) != cudaSuccess)
+    return SKN_ERR_CUDA;
+  k_eigvec<<<vec_grid(n_prob), VNT, vsmem, stream>>>(n_prob, n, hs_off, eig_off, order, (const double2*)H,
+                                                     (const double2*)S, eig, tri, status, (double2*)vec, scratch,
+                                                     work_counter + 1, mn);
   return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
 }
