@@ -11,6 +11,7 @@ sums -> eigensolve -> Fermi/gap -> DOS.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence
@@ -274,7 +275,16 @@ class BatchResult:
     dos: torch.Tensor            # [S, npts]
     H: Optional[torch.Tensor] = None
     S: Optional[torch.Tensor] = None
+    vec: Optional[torch.Tensor] = None   # complex128, problem p at hs_off[p], row-major [component][band]
     timings: dict = field(default_factory=dict)
+
+    def eigenvectors(self, s: int) -> torch.Tensor:
+        """[nk, n, n] complex: [k, i, j] = component i of eigenvector j (ascending eigenvalues)."""
+        p = self.plan
+        n = int(p.nb[s])
+        q = np.nonzero(p.prob_struct == s)[0]
+        o = int(p.hs_off[q[0]])
+        return self.vec[o: o + len(q) * n * n].view(len(q), n, n)
 
     def eigenvalues(self, s: int) -> torch.Tensor:
         p = self.plan
@@ -321,7 +331,8 @@ class DeviceBatch:
 
 # kernels each ABI call launches (for the launch count the bench reports)
 KERNELS_PER_CALL = {"skn_bond_counts": 1, "skn_bond_fill": 1, "skn_image_phases": 1, "skn_sk_blocks": 1,
-                    "skn_bloch": 1, "skn_eigh_gen_batched": 1, "skn_fermi_gap": 1, "skn_dos": 2}
+                    "skn_bloch": 1, "skn_eigh_gen_batched": 1, "skn_eigh_gen_vectors": 2, "skn_fermi_gap": 1,
+                    "skn_dos": 2}
 
 
 class Engine:
@@ -349,15 +360,17 @@ class Engine:
         self.launches += KERNELS_PER_CALL.get(name, 1)
 
     def run(self, plan: Plan, dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
-            dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False) -> BatchResult:
+            dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False,
+            vectors: bool = False) -> BatchResult:
         with torch.cuda.device(self.device):
             ctx = torch.cuda.stream(self.stream) if self.stream is not None else _nullctx()
             with ctx:
                 db = DeviceBatch(plan, self.device)
-                return self.execute(db, dos_range, dos_points, dos_sigma, dos_window, keep_hs, hs_only)
+                return self.execute(db, dos_range, dos_points, dos_sigma, dos_window, keep_hs, hs_only, vectors)
 
     def execute(self, db: DeviceBatch, dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
-                dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False) -> BatchResult:
+                dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False,
+                vectors: bool = False) -> BatchResult:
         """Kernels only, on the current stream; one device->host read sizes the bond table."""
         plan = db.plan
         dev = self.device
@@ -410,9 +423,21 @@ class Engine:
             return BatchResult(plan, None, None, None, None, None, None, None, hs_copy[0], hs_copy[1])
         eig = torch.empty(max(plan.eig_total, 1), dtype=torch.float64, device=dev)
         eig_status = torch.empty(max(n_prob, 1), dtype=torch.int32, device=dev)
-        counter = torch.zeros(1, dtype=torch.int32, device=dev)
-        self._call("skn_eigh_gen_batched", n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order), ptr(Hk),
-                   ptr(Sk), ptr(eig), ptr(eig_status), ptr(counter), plan.max_n, stream)
+        counter = torch.zeros(2, dtype=torch.int32, device=dev)
+        vec = None
+        if vectors:
+            vec = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
+            tri = torch.empty(4 * max(plan.eig_total, 1), dtype=torch.float64, device=dev)
+            need = ctypes.c_int64(0)
+            call("skn_eigh_vectors_scratch_bytes", n_prob, plan.max_n, ctypes.addressof(need))
+            scratch = torch.empty(max(need.value // 8, 1), dtype=torch.float64, device=dev)
+            self._call("skn_eigh_gen_vectors", n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order),
+                       ptr(Hk), ptr(Sk), ptr(eig), ptr(vec), ptr(eig_status), ptr(tri), ptr(scratch),
+                       int(need.value), ptr(counter), plan.max_n, stream)
+            vec = torch.view_as_complex(vec.view(-1, 2))
+        else:
+            self._call("skn_eigh_gen_batched", n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order),
+                       ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counter), plan.max_n, stream)
         mu = torch.empty(S, dtype=torch.float64, device=dev)
         stats = torch.zeros(S * _lib.SKN_NSTAT, dtype=torch.float64, device=dev)
         fst = torch.empty(S, dtype=torch.int32, device=dev)
@@ -424,7 +449,7 @@ class Engine:
                    float(dos_range[0]), float(dos_range[1]), int(dos_points), float(dos_sigma), float(dos_window),
                    ptr(grid), ptr(dos), ptr(stats), stream)
         return BatchResult(plan, eig, eig_status, mu, stats.view(S, _lib.SKN_NSTAT), fst, grid,
-                           dos.view(S, dos_points), hs_copy[0], hs_copy[1])
+                           dos.view(S, dos_points), hs_copy[0], hs_copy[1], vec)
 
     def check_tables(self):
         """Raise if the last execute() needed a table the parameter set lacks (reads one device int)."""

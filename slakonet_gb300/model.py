@@ -236,7 +236,8 @@ class MultiElementSkfParameterOptimizer(nn.Module):
     # ----------------------------------------------------------- properties
     def compute_properties_batch(self, structures: Sequence[dict], shell_dict=None, device=None,
                                  dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
-                                 dos_window: float = 0.0, cutoff: float = E.CUTOFF_BOHR, engine=None):
+                                 dos_window: float = 0.0, cutoff: float = E.CUTOFF_BOHR, engine=None,
+                                 with_eigenvectors: bool = False):
         """Batched path: many structures (each with its own k-points) in one launch sequence.
 
         Each structure is a dict with ``numbers``, ``positions`` and ``cell``
@@ -249,7 +250,7 @@ class MultiElementSkfParameterOptimizer(nn.Module):
         ts = self.table_set(shell_dict, device, zs)
         eng = engine or E.Engine(ts, cutoff)
         plan = E.plan_batch(structures, ts, cutoff)
-        res = eng.run(plan, dos_range, dos_points, dos_sigma, dos_window)
+        res = eng.run(plan, dos_range, dos_points, dos_sigma, dos_window, vectors=with_eigenvectors)
         eng.check_tables()
         return res
 
@@ -259,8 +260,6 @@ class MultiElementSkfParameterOptimizer(nn.Module):
         """Reference signature (slakonet/optim.py:949-962); returns ``(properties, True)``."""
         if phonons or get_energy or get_forces or get_bulk_mod:
             raise NotImplementedError("phonons, total energy, forces and bulk modulus are outside this path")
-        if with_eigenvectors:
-            raise NotImplementedError("eigenvectors are not produced by this path yet")
         if device is None:
             device = "cuda"
         device = torch.device(device)
@@ -274,7 +273,7 @@ class MultiElementSkfParameterOptimizer(nn.Module):
             k = mp_kpoints([1, 1, 1])
         st["kpoints"] = k
         st["weights"] = np.full(len(k), 1.0 / len(k))
-        res = self.compute_properties_batch([st], shell_dict, device)
+        res = self.compute_properties_batch([st], shell_dict, device, with_eigenvectors=with_eigenvectors)
         return properties_dict(res, 0, get_fermi=get_fermi), True
 
 
@@ -327,8 +326,9 @@ def properties_dict(res: "E.BatchResult", s: int, get_fermi: bool = False) -> di
         k_weights=torch.as_tensor(plan.kweights[k0:k0 + nk]).unsqueeze(0),
         kpoints=torch.as_tensor(plan.kpoints[k0:k0 + nk]).unsqueeze(0),
         nelectron=torch.tensor([plan.nelec[s]]),
-        eig_status=res.eig_status[plan.prob_struct == s] if False else None,
     )
+    if res.vec is not None:   # reference layout [1, n (component), n (band), nk]
+        calc.eigenvectors = res.eigenvectors(s).permute(1, 2, 0).unsqueeze(0)
     if get_fermi:
         props["efermi"] = (res.mu[s] * H2E).reshape(1, 1, 1)
         props["bandgap"] = res.stats[s, I["bandgap_ev"]].reshape(1)
