@@ -203,6 +203,59 @@ int skn_dos(int n_struct, const int64_t* eig_off, const int32_t* nk, const int32
             double* grid, double* dos, double* stats, cudaStream_t stream);
 
 /*
+ * Adjoint, step 1: weighted eigenvector projectors per problem,
+ *   G_ab = sum_n g_n conj(c_n[a]) c_n[b],  F_ab = sum_n g_n e_n conj(c_n[a]) c_n[b],
+ * from eigenvectors `vec` (skn_eigh_gen_vectors layout), eigenvalues and
+ * grad_eig = dL/de; G, F column-major complex at hs_off[p].  With these,
+ * dL/dH(k) = G and dL/dS(k) = -F.  Replaces the eigenvalue part of
+ * _SymEigB.backward (slakonet/utils.py:387-473), whose complex case omits
+ * the conjugate of the eigenvectors.
+ */
+int skn_adj_projectors(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                       const double* vec, const double* eig, const double* grad_eig, double* G, double* F,
+                       cudaStream_t stream);
+
+/*
+ * Adjoint, step 2: dL/dB for every bond's real-space H and S block,
+ * dL/dB_ab(T) = sum_k Re(G_ab(k) exp(i 2 pi k.T)) (S: -F), written in the
+ * block layout of skn_sk_blocks.  The autograd counterpart is the backward of
+ * _pe_sk_data2's phase multiply and scatter (slakonet/slaterkoster.py:971-1010).
+ *   atom_struct[A], struct_prob0[S] (first problem of each structure; a
+ *   structure's problems are consecutive, k-ordered), nk[S], nb[S].
+ */
+int skn_adj_bloch(int64_t n_bonds, const int32_t* bond_i, const int32_t* bond_j, const int32_t* bond_img,
+                  const int64_t* bond_blk, const int32_t* atom_struct, const int32_t* atom_orb_off,
+                  const int32_t* atom_norb, const int32_t* struct_prob0, const int32_t* nk, const int32_t* nb,
+                  const int64_t* hs_off, const int32_t* image_range, const int64_t* phase_base, const double* phases,
+                  const double* G, const double* F, double* grad_blk_H, double* grad_blk_S, cudaStream_t stream);
+
+/*
+ * Adjoint, step 3: pull the block gradients back through the rotation and
+ * the 8-point spline (or the tail functional) onto the packed tables,
+ * accumulating into grad_tab_H / grad_tab_S (same layout as tab_H / tab_S;
+ * zero them first).  The autograd counterpart is the backward of
+ * sub_block_rot and PolyInterpU (slakonet/slaterkoster.py:1013-1122,
+ * slakonet/interpolation.py:107-311).
+ */
+int skn_adj_tables(int64_t n_bonds, const int32_t* bond_i, const int32_t* bond_j, const double* bond_d,
+                   const double* bond_u, const int64_t* bond_blk, const int32_t* atom_species, int n_species,
+                   const int32_t* sp_nshell, const int32_t* sp_shell_l, const int32_t* sp_norb,
+                   const int32_t* tab_index, const int64_t* tab_off, const int32_t* tab_ngrid, const double* tab_step,
+                   const double* grad_blk_H, const double* grad_blk_S, double* grad_tab_H, double* grad_tab_S,
+                   cudaStream_t stream);
+
+/*
+ * DOS backward: grad_eig[e] += dL/de from grad_dos = dL/dDOS of skn_dos with
+ * the same grid arguments (mu held fixed, as the reference detaches it in
+ * fermi_search, slakonet/fermi.py:191-196).  max_count = max over
+ * structures of nk * nb.
+ */
+int skn_dos_backward(int n_struct, const int64_t* eig_off, const int32_t* nk, const int32_t* nb,
+                     const int64_t* kw_off, const double* kweights, const double* eig, const double* mu,
+                     double e_lo, double e_hi, int npts, double sigma, double window_sigmas,
+                     const double* grad_dos, double* grad_eig, int max_count, cudaStream_t stream);
+
+/*
  * FP64 fused multiply-add throughput probe (no counterpart in the reference):
  * blocks x 256 threads, 8 independent FMA chains of `iters` steps each,
  * 16 * iters flops per thread, result written to out[blocks*256].  Used to

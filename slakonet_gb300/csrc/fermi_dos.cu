@@ -31,7 +31,7 @@ enum {
   ST_MU_HA = 0, ST_FERMI_EV = 1, ST_GAP_EV = 2, ST_VBM_EV = 3, ST_CBM_EV = 4, ST_DIRECT = 5,
   ST_VBM_K = 6, ST_CBM_K = 7, ST_VWIDTH = 8, ST_CWIDTH = 9, ST_MIN_DGAP = 10, ST_DIRECT_SEMI = 11,
   ST_EFERMI_EV = 12, ST_BANDGAP_EV = 13, ST_CONVERGED = 14, ST_ITERS = 15, ST_DOS_FERMI = 16,
-  ST_DOS_GAPC = 17, ST_DOS_TOTAL = 18, ST_METAL = 19, ST_FALLBACK = 20
+  ST_DOS_GAPC = 17, ST_DOS_TOTAL = 18, ST_METAL = 19, ST_FALLBACK = 20, ST_VBM_FLAT = 21, ST_CBM_FLAT = 22
 };
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }
@@ -192,6 +192,8 @@ __global__ void __launch_bounds__(NT) k_fermi_gap(const int64_t* __restrict__ ei
       st[ST_DIRECT] = (vk == ck) ? 1.0 : 0.0;
       st[ST_VBM_K] = vk; st[ST_CBM_K] = ck; st[ST_FALLBACK] = 0.0;
     }
+    st[ST_VBM_FLAT] = (metal || nocc == 0 || nunocc == 0) ? -1.0 : (double)vbi;
+    st[ST_CBM_FLAT] = (metal || nocc == 0 || nunocc == 0) ? -1.0 : (double)cbi;
     st[ST_EFERMI_EV] = mu * H2E;
     const double bg = gc - gv;
     st[ST_BANDGAP_EV] = (bg > 0.0 ? bg : (bg == bg ? 0.0 : bg)) * H2E;

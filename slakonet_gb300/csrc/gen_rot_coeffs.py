@@ -50,8 +50,8 @@ def main():
                 rows.append(weights(l, m, n))
                 cnt += 1
     print(f"#define SKN_ROT_NENT {cnt}")
-    print(f"__device__ const int SKN_ROT_OFF[4] = {{0, 0, {off[2]}, {off[3]}}};")
-    print("__device__ const double SKN_ROT_W[SKN_ROT_NENT * 5] = {")
+    print(f"static __device__ const int SKN_ROT_OFF[4] = {{0, 0, {off[2]}, {off[3]}}};")
+    print("static __device__ const double SKN_ROT_W[SKN_ROT_NENT * 5] = {")
     for r in rows:
         print("  " + ", ".join(repr(float(x)) for x in r) + ",")
     print("};")

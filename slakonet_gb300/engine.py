@@ -29,7 +29,7 @@ KT_FERMI = 0.01             # fermi_search default (slakonet/fermi.py:143)
 # stats record layout (mirrors csrc/fermi_dos.cu)
 STAT = dict(mu_ha=0, fermi_ev=1, gap_ev=2, vbm_ev=3, cbm_ev=4, direct=5, vbm_k=6, cbm_k=7, vwidth=8,
             cwidth=9, min_dgap=10, direct_semi=11, efermi_ev=12, bandgap_ev=13, converged=14, iters=15,
-            dos_fermi=16, dos_gapc=17, dos_total=18, metal=19, fallback=20)
+            dos_fermi=16, dos_gapc=17, dos_total=18, metal=19, fallback=20, vbm_flat=21, cbm_flat=22)
 
 
 def _dev(device) -> torch.device:
@@ -81,6 +81,7 @@ class TableSet:
             sp_norb[i] = sum(2 * l + 1 for l in ls)
         tab_index = -np.ones(16 * nsp * nsp, np.int32)
         offs, ngrid, stepv, hs, ss = [], [], [], [], []
+        self.param_slices = []   # (tensor, "H"|"S", offset, numel) in packing order
         off = 0
         for a, za in enumerate(self.species):
             for b, zb in enumerate(self.species):
@@ -94,6 +95,10 @@ class TableSet:
                     tab_index[((a * nsp + b) * 4 + l1) * 4 + l2] = t
                     if th.shape[-1] < 9:
                         raise ValueError(f"table ({za},{zb},{l1},{l2}) has {th.shape[-1]} grid points; 9 needed")
+                    if isinstance(th, torch.Tensor):
+                        self.param_slices.append((th, "H", off, th.numel()))
+                    if isinstance(ts, torch.Tensor):
+                        self.param_slices.append((ts, "S", off, ts.numel()))
                     th = torch.as_tensor(th).detach().to(self.device, torch.float64)
                     ts = torch.as_tensor(ts).detach().to(self.device, torch.float64)
                     offs.append(off)
@@ -277,6 +282,7 @@ class BatchResult:
     S: Optional[torch.Tensor] = None
     vec: Optional[torch.Tensor] = None   # complex128, problem p at hs_off[p], row-major [component][band]
     timings: dict = field(default_factory=dict)
+    state: Optional[dict] = None
 
     def eigenvectors(self, s: int) -> torch.Tensor:
         """[nk, n, n] complex: [k, i, j] = component i of eigenvector j (ascending eigenvalues)."""
@@ -370,7 +376,7 @@ class Engine:
 
     def execute(self, db: DeviceBatch, dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
                 dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False,
-                vectors: bool = False) -> BatchResult:
+                vectors: bool = False, keep_state: bool = False) -> BatchResult:
         """Kernels only, on the current stream; one device->host read sizes the bond table."""
         plan = db.plan
         dev = self.device
@@ -448,8 +454,14 @@ class Engine:
         self._call("skn_dos", S, ptr(db.eos), ptr(db.nk), ptr(db.nb), ptr(db.kwoff), ptr(db.kw), ptr(eig), ptr(mu),
                    float(dos_range[0]), float(dos_range[1]), int(dos_points), float(dos_sigma), float(dos_window),
                    ptr(grid), ptr(dos), ptr(stats), stream)
-        return BatchResult(plan, eig, eig_status, mu, stats.view(S, _lib.SKN_NSTAT), fst, grid,
-                           dos.view(S, dos_points), hs_copy[0], hs_copy[1], vec)
+        out = BatchResult(plan, eig, eig_status, mu, stats.view(S, _lib.SKN_NSTAT), fst, grid,
+                          dos.view(S, dos_points), hs_copy[0], hs_copy[1], vec)
+        if keep_state:
+            out.state = dict(bond_i=bond_i, bond_j=bond_j, bond_img=bond_img, bond_d=bond_d, bond_u=bond_u,
+                             bond_blk=bond_blk, nbond=nbond, nblk=nblk, phases=phases, db=db,
+                             dos_args=(float(dos_range[0]), float(dos_range[1]), int(dos_points), float(dos_sigma),
+                                       float(dos_window)))
+        return out
 
     def check_tables(self):
         """Raise if the last execute() needed a table the parameter set lacks (reads one device int)."""

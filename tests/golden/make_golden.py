@@ -212,7 +212,103 @@ def fixture_fermi():
     np.savez_compressed(os.path.join(HERE, "fermi.npz"), **cases)
 
 
+def _fixed_symeig_backward(ctx, w_bar, v_bar):
+    """_SymEigB.backward (slakonet/utils.py:387-473) with the eigenvector conjugate restored."""
+    w, v = ctx.saved_tensors
+    bf = ctx.bf
+    vh = v.conj().transpose(-2, -1)
+    out = v @ torch.diag_embed(w_bar.to(v.dtype)) @ vh
+    if v_bar is not None:
+        d = w.unsqueeze(-2) - w.unsqueeze(-1)
+        d = torch.where(d.abs() > bf, d, torch.full_like(d, bf) * torch.sign(d))
+        Fm = torch.where(torch.eye(w.shape[-1], dtype=torch.bool), torch.zeros_like(d), 1.0 / d)
+        x = Fm.to(v.dtype) * (vh @ v_bar)
+        out = out + v @ ((x + x.conj().transpose(-2, -1)) / 2) @ vh
+    return out, None, None
+
+
+def _reference_grads(model, st, sd, kpoints, fixed):
+    """Gradients of L = sum sin(5 e + 0.3) over all (k, band) eigenvalues (Hartree)."""
+    orig = ref.utils._SymEigB.backward
+    if fixed:
+        ref.utils._SymEigB.backward = staticmethod(_fixed_symeig_backward)
+    try:
+        model.zero_grad()
+        with inject_kpoints(kpoints):
+            props, _ = model.compute_multi_element_properties(geometry=geometry(st), shell_dict=sd, device="cpu")
+        eig = props["eigenvalues"]
+        loss = torch.sin(5.0 * eig + 0.3).sum()
+        loss.backward()
+    finally:
+        ref.utils._SymEigB.backward = orig
+    out = {}
+    for key, opt in model.skf_optimizers.items():
+        for kind, pd in (("h", opt.h_params), ("s", opt.s_params)):
+            for lk, prm in pd.items():
+                out[f"{key}|{kind}|{lk}"] = (prm.grad.detach().numpy().copy() if prm.grad is not None
+                                             else np.zeros(tuple(prm.shape)))
+    return out, float(loss.detach())
+
+
+def _reference_loss(model, st, sd, kpoints):
+    with torch.no_grad(), inject_kpoints(kpoints):
+        props, _ = model.compute_multi_element_properties(geometry=geometry(st), shell_dict=sd, device="cpu")
+    return float(torch.sin(5.0 * props["eigenvalues"] + 0.3).sum())
+
+
+def fixture_gradients():
+    """Reference autograd (shipped and conjugate-restored) plus central differences, h = 1e-5."""
+    cases = []
+    sd = {14: [0, 1, 2]}
+    tables = syn.make_tables([14], sd, seed=0)
+    cases.append(("grad_si", tables, syn.diamond_si(), sd, np.array([[0.1, 0.2, 0.3], [0.0, 0.0, 0.0],
+                                                                    [0.25, 0.5, 0.125]]), {"seed": 0,
+                                                                                           "shells": np.array([0, 1, 2])}))
+    rng = np.random.default_rng(31)
+    st = syn.random_structure(rng, 3, zmax=30)
+    st["numbers"] = np.array([1, 26, 14])
+    sd_all = syn.default_shell_dict()
+    tables2 = syn.make_tables(st["numbers"], sd_all, seed=9)
+    cases.append(("grad_hetero", tables2, st, {int(z): sd_all[int(z)] for z in st["numbers"]},
+                  np.array([[0.0, 0.0, 0.0], [0.3, -0.2, 0.1]]), {"table_seed": 9}))
+    for name, tb, stx, sdx, kp, extra in cases:
+        model = build_reference_model(ref, tb)
+        g_ship, loss = _reference_grads(model, stx, sdx, kp, fixed=False)
+        g_fix, _ = _reference_grads(model, stx, sdx, kp, fixed=True)
+        # central differences on the entries with the largest fixed gradients
+        keys = sorted(g_fix, key=lambda k: -np.abs(g_fix[k]).max())[:3]
+        fd = []
+        for key in keys:
+            pair, kind, lk = key.split("|")
+            prm = getattr(model.skf_optimizers[pair], f"{kind}_params")[lk]
+            idx = np.unravel_index(np.argmax(np.abs(g_fix[key])), g_fix[key].shape)
+            with torch.no_grad():
+                old = prm[idx].item()
+                prm[idx] = old + 1e-5
+                lp = _reference_loss(model, stx, sdx, kp)
+                prm[idx] = old - 1e-5
+                lm = _reference_loss(model, stx, sdx, kp)
+                prm[idx] = old
+            fd.append((key, idx, (lp - lm) / 2e-5, g_fix[key][idx], g_ship[key][idx]))
+        payload = {"kpoints": kp, "numbers": stx["numbers"], "positions": stx["positions"], "cell": stx["cell"],
+                   "loss": loss, "tables_checksum": tables_checksum(tb)}
+        payload.update(extra)
+        for k, v in g_fix.items():
+            payload["fixed|" + k] = v
+            payload["shipped|" + k] = g_ship[k]
+        payload["fd_keys"] = np.array([f[0] for f in fd])
+        payload["fd_idx"] = np.array([list(f[1]) for f in fd])
+        payload["fd_values"] = np.array([[f[2], f[3], f[4]] for f in fd])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **payload)
+        print(name, "FD | fixed autograd | shipped autograd:")
+        for f in fd:
+            print("  ", f[0], f[1], f"{f[2]: .6e} {f[3]: .6e} {f[4]: .6e}")
+
+
 if __name__ == "__main__":
+    if "--gradients-only" in sys.argv:
+        fixture_gradients()
+        sys.exit(0)
     fixture_interp()
     fixture_blocks()
     fixture_fermi()
@@ -222,4 +318,5 @@ if __name__ == "__main__":
     fixture_random("rand_a", 6, 21, 21, zmax=30)
     fixture_random("rand_b", 9, 22, 22)
     fixture_random("rand_c", 3, 23, 23)
+    fixture_gradients()
     print("golden fixtures written to", HERE)
