@@ -78,6 +78,7 @@ def adjoint(eng: "E.Engine", res: "E.BatchResult", g_eig=None, g_dos=None, g_gap
         ic = (base + cf.clamp(min=0).long())[ok]
         g.index_add_(0, iv, -gg[ok])
         g.index_add_(0, ic, gg[ok])
+    st["degenerate_pairs"] = _degenerate_pairs(plan, res.eig, g)
     n_prob = len(plan.prob_n)
     Gm = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
     Fm = torch.empty_like(Gm)
@@ -107,6 +108,26 @@ def adjoint(eng: "E.Engine", res: "E.BatchResult", g_eig=None, g_dos=None, g_gap
         src = dtab_H if kind == "H" else dtab_S
         grads.append(src[off: off + numel].view(tensor.shape).to(tensor.device))
     return grads
+
+
+def _degenerate_pairs(plan, eig, g, tol: float = 1e-8) -> int:
+    """Adjacent bands at one k closer than ``tol`` Hartree whose loss weights differ.
+
+    For such a pair the derivative of each eigenvalue separately is not
+    defined; the projector form used here returns the derivative of the
+    weighted sum over the degenerate subspace, which is exact only when the
+    weights agree.  The count is reported so callers can tell.
+    """
+    if plan.eig_total < 2:
+        return 0
+    nb = np.repeat(plan.nb, plan.nk.astype(np.int64) * plan.nb)
+    pos = np.concatenate([np.arange(int(k) * int(b)) % int(b) for k, b in zip(plan.nk, plan.nb)])
+    valid = torch.as_tensor((pos[:-1] < nb[:-1] - 1), device=eig.device)
+    de = (eig[1:plan.eig_total] - eig[:plan.eig_total - 1]).abs()
+    dg = (g[1:plan.eig_total] - g[:plan.eig_total - 1]).abs()
+    gscale = float(g.abs().max()) if plan.eig_total else 0.0
+    flag = valid & (de < tol) & (dg > 1e-9 * max(gscale, 1e-300))
+    return int(flag.sum())
 
 
 def differentiable_properties(model, structures: Sequence[dict], shell_dict=None, device="cuda",

@@ -857,6 +857,23 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
 }
 }  // namespace
 
+// Dynamic shared-memory limits are per-function attributes.  They are set to
+// the largest size any call can request (max_n = MAX_N), so concurrent calls
+// from several host threads never lower the limit under another's launch.
+static size_t eig_smem_bytes(int mn) {
+  return sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn) +
+         2 * SMEM_LDA * SMEM_N * sizeof(double2);
+}
+static size_t vec_smem_bytes(int mn) {
+  return sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;
+}
+static cudaError_t set_smem_limit_once() {
+  cudaError_t e = cudaFuncSetAttribute(k_eigh_gen, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)eig_smem_bytes(MAX_N));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_eigvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_smem_bytes(MAX_N));
+}
+
 extern "C" int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
                                     const int32_t* order, double* H, double* S, double* eig, int32_t* status,
                                     int32_t* work_counter, int max_n, cudaStream_t stream) {
@@ -868,8 +885,7 @@ extern "C" int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t*
   const int use_smem_mats = 1;
   size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn);
   smem += (size_t)use_smem_mats * 2 * SMEM_LDA * SMEM_N * sizeof(double2);
-  if (cudaFuncSetAttribute(k_eigh_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return SKN_ERR_CUDA;
+  if (set_smem_limit_once() != cudaSuccess) return SKN_ERR_CUDA;
   int per_sm = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -914,8 +930,7 @@ extern "C" int skn_eigh_gen_vectors(int n_prob, const int32_t* n, const int64_t*
   const int use_smem_mats = 1;
   size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn);
   smem += (size_t)use_smem_mats * 2 * SMEM_LDA * SMEM_N * sizeof(double2);
-  if (cudaFuncSetAttribute(k_eigh_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return SKN_ERR_CUDA;
+  if (set_smem_limit_once() != cudaSuccess) return SKN_ERR_CUDA;
   int per_sm = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -928,8 +943,7 @@ extern "C" int skn_eigh_gen_vectors(int n_prob, const int32_t* n, const int64_t*
                                          work_counter, mn, use_smem_mats, tri);
   if (cudaPeekAtLastError() != cudaSuccess) return SKN_ERR_CUDA;
   const size_t vsmem = sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;
-  if (cudaFuncSetAttribute(k_eigvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem) != cudaSuccess)
-    return SKN_ERR_CUDA;
+
   k_eigvec<<<vec_grid(n_prob), VNT, vsmem, stream>>>(n_prob, n, hs_off, eig_off, order, (const double2*)H,
                                                      (const double2*)S, eig, tri, status, (double2*)vec, scratch,
                                                      work_counter + 1, mn);

@@ -1,0 +1,236 @@
+"""Continuous-batching server for the properties path.
+
+Requests (one periodic structure each) arrive at any time.  A request is
+admitted when its device-memory estimate fits the budget left by requests
+already admitted; admitted requests wait in a queue.  Each worker thread owns
+a CUDA stream: it takes every request that is admitted and not yet started
+(up to ``max_batch_problems`` (structure, k) problems), plans them as one
+batch, runs the whole path on its stream, copies the results to the host and
+releases their memory.  With two or more workers, a batch formed from
+requests that arrived while another batch was on the GPU runs concurrently
+with it, so arrivals never wait for a whole batch to drain.
+
+The reference serves one structure per call (slakonet/optim.py:949-1075 via
+predict_slakonet.py); there is no queue, batch or stream there.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Dict, List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import engine as E
+from .model import MultiElementSkfParameterOptimizer, properties_dict
+
+MAX_N = 2048   # single-CTA eigensolver bound (csrc/eigh.cu)
+
+
+def request_bytes(n_orb: int, nk: int, dos_points: int) -> int:
+    """Device bytes one request holds while in flight (H, S, eigenvalues, DOS, slack for bonds)."""
+    return int(2 * 16 * n_orb * n_orb * nk + 8 * n_orb * nk + 8 * dos_points + (8 << 20))
+
+
+@dataclass
+class Request:
+    rid: int
+    structure: dict
+    n_orb: int
+    nk: int
+    nbytes: int
+    t_submit: float
+    future: cf.Future = field(default_factory=cf.Future)
+    t_start: float = 0.0
+    t_done: float = 0.0
+
+
+class Admission:
+    """Memory-budget admission (host-side, thread-safe)."""
+
+    def __init__(self, budget_bytes: int):
+        self.budget = int(budget_bytes)
+        self.used = 0
+        self.lock = threading.Lock()
+
+    def try_admit(self, nbytes: int) -> bool:
+        with self.lock:
+            if self.used + nbytes <= self.budget or self.used == 0:
+                self.used += nbytes
+                return True
+            return False
+
+    def release(self, nbytes: int):
+        with self.lock:
+            self.used -= nbytes
+
+
+class Server:
+    """Continuous-batching front end of ``MultiElementSkfParameterOptimizer``."""
+
+    def __init__(self, model: MultiElementSkfParameterOptimizer, shell_dict: Dict[int, List[int]], device="cuda",
+                 species: Optional[Sequence[int]] = None, mem_budget_bytes: Optional[int] = None,
+                 n_workers: int = 2, max_batch_problems: int = 8192, dos_range=(-20.0, 10.0),
+                 dos_points: int = 1000, dos_sigma: float = 0.1, dos_window: float = 9.0,
+                 executor: Optional[Callable] = None):
+        self.model = model
+        self.sd = shell_dict
+        self.device = torch.device(device)
+        self.dos = dict(dos_range=dos_range, dos_points=dos_points, dos_sigma=dos_sigma, dos_window=dos_window)
+        self.max_batch_problems = max_batch_problems
+        if mem_budget_bytes is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            mem_budget_bytes = int(0.6 * free)
+        self.adm = Admission(mem_budget_bytes)
+        self.tables = model.table_set(shell_dict, self.device, species) if executor is None else None
+        if self.tables is not None:
+            torch.cuda.synchronize(self.device)   # tables are read by every worker stream
+        self.executor = executor or self._execute
+        self.pending: "queue.Queue[Request]" = queue.Queue()     # submitted, not admitted
+        self.ready: List[Request] = []                            # admitted, not started
+        self.cv = threading.Condition()
+        self.stop = False
+        self.rid = 0
+        self.workers = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(n_workers)]
+        self.admitter = threading.Thread(target=self._admit_loop, daemon=True)
+        self.batches = 0
+        self.rejected = 0
+        for w in self.workers:
+            w.start()
+        self.admitter.start()
+
+    # ------------------------------------------------------------ clients
+    def submit(self, structure: dict) -> cf.Future:
+        n_orb = sum(sum(2 * l + 1 for l in self.sd[int(z)]) for z in np.asarray(structure["numbers"]).reshape(-1))
+        nk = len(structure["kpoints"])
+        with self.cv:
+            self.rid += 1
+            req = Request(self.rid, structure, n_orb, nk, request_bytes(n_orb, nk, self.dos["dos_points"]),
+                          time.perf_counter())
+        if n_orb > MAX_N:
+            self.rejected += 1
+            req.future.set_exception(ValueError(f"{n_orb} orbitals exceed the eigensolver's {MAX_N}"))
+            return req.future
+        self.pending.put(req)
+        return req.future
+
+    def close(self):
+        with self.cv:
+            self.stop = True
+            self.cv.notify_all()
+        self.pending.put(None)
+        for w in self.workers:
+            w.join()
+        self.admitter.join()
+
+    # ------------------------------------------------------------ internals
+    def _admit_loop(self):
+        waiting: Optional[Request] = None
+        while True:
+            if waiting is None:
+                waiting = self.pending.get()
+                if waiting is None:
+                    return
+            if self.adm.try_admit(waiting.nbytes):
+                with self.cv:
+                    self.ready.append(waiting)
+                    self.cv.notify()
+                waiting = None
+            else:
+                time.sleep(0.0005)
+                with self.cv:
+                    if self.stop:
+                        return
+
+    def _take_batch(self) -> List[Request]:
+        with self.cv:
+            while not self.ready and not self.stop:
+                self.cv.wait(0.05)
+            if not self.ready:
+                return []
+            batch, probs = [], 0
+            while self.ready and (not batch or probs + self.ready[0].nk <= self.max_batch_problems):
+                r = self.ready.pop(0)
+                probs += r.nk
+                batch.append(r)
+            return batch
+
+    def _execute(self, structures, stream):
+        with torch.cuda.stream(stream):
+            eng = E.Engine(self.tables, stream=stream)
+            plan = E.plan_batch(structures, self.tables)
+            db = E.DeviceBatch(plan, self.device)
+            res = eng.execute(db, **self.dos)
+            eng.check_tables()
+            out = []
+            eig = res.eig.to("cpu", non_blocking=False)
+            dos = res.dos.to("cpu")
+            stats = res.stats.to("cpu")
+            mu = res.mu.to("cpu")
+            status = res.eig_status.to("cpu")
+            for s in range(plan.n_struct):
+                o, nk, nb = int(plan.eig_off_struct[s]), int(plan.nk[s]), int(plan.nb[s])
+                ok = status[plan.prob_struct == s]
+                out.append({"eigenvalues": eig[o:o + nk * nb].view(nk, nb), "dos": dos[s], "stats": stats[s],
+                            "fermi_energy_Ha": float(mu[s]), "band_gap_eV": float(stats[s, E.STAT["gap_ev"]]),
+                            "eig_status_ok": bool((ok == 0).all())})
+            return out
+
+    def _worker(self, idx: int):
+        stream = torch.cuda.Stream(self.device) if self.executor == self._execute else None
+        while True:
+            batch = self._take_batch()
+            if not batch:
+                with self.cv:
+                    if self.stop and not self.ready:
+                        return
+                continue
+            t0 = time.perf_counter()
+            for r in batch:
+                r.t_start = t0
+            try:
+                outs = self.executor([r.structure for r in batch], stream)
+                err = None
+            except Exception as e:   # surfaced on every request of the batch
+                outs, err = None, e
+            t1 = time.perf_counter()
+            self.batches += 1
+            for i, r in enumerate(batch):
+                r.t_done = t1
+                self.adm.release(r.nbytes)
+                if err is not None:
+                    r.future.set_exception(err)
+                else:
+                    res = outs[i]
+                    res["latency_s"] = t1 - r.t_submit
+                    r.future.set_result(res)
+
+
+def poisson_stream(server: Server, structures: Sequence[dict], rate: float, seed: int = 0):
+    """Submit ``structures`` with exponential inter-arrival times (mean 1/rate); wait for all.
+
+    Returns (latencies_s [array], wall_s, results)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, len(structures))
+    t0 = time.perf_counter()
+    due = t0
+    futs = []
+    for st, gsec in zip(structures, gaps):
+        due += gsec
+        now = time.perf_counter()
+        if due > now:
+            time.sleep(due - now)
+        futs.append(server.submit(st))
+    results = []
+    for f in futs:
+        try:
+            results.append(f.result())
+        except Exception as e:   # rejected requests
+            results.append({"error": str(e)})
+    wall = time.perf_counter() - t0
+    lat = np.array([r["latency_s"] for r in results if "latency_s" in r])
+    return lat, wall, results

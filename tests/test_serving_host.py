@@ -1,0 +1,79 @@
+"""Serving control logic on the CPU with a fake executor (no GPU)."""
+import threading
+import time
+
+import numpy as np
+
+from slakonet_gb300 import serving as SV, synthetic as syn
+
+
+class FakeModel:
+    pass
+
+
+def _structs(n, seed=0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        st = syn.random_structure(rng, int(rng.integers(1, 6)), zmax=20)
+        st["kpoints"] = np.zeros((int(rng.integers(1, 5)), 3))
+        out.append(st)
+    return out
+
+
+def test_admission_budget_never_exceeded_and_all_requests_complete():
+    peak = {"v": 0}
+    live = {"v": 0}
+    lock = threading.Lock()
+
+    def fake_exec(structures, stream):
+        with lock:
+            live["v"] += len(structures)
+            peak["v"] = max(peak["v"], server.adm.used)
+        time.sleep(0.01)
+        with lock:
+            live["v"] -= len(structures)
+        return [{"eigenvalues": np.zeros(1), "band_gap_eV": 0.0} for _ in structures]
+
+    sd = syn.default_shell_dict()
+    sts = _structs(60)
+    budget = 3 * SV.request_bytes(16, 4, 1000)
+    server = SV.Server(FakeModel(), sd, device="cpu", mem_budget_bytes=budget, n_workers=3, executor=fake_exec)
+    lat, wall, res = SV.poisson_stream(server, sts, rate=2000.0, seed=1)
+    server.close()
+    assert len(lat) == len(sts)
+    assert peak["v"] <= budget
+    assert server.adm.used == 0
+    assert server.batches >= 2
+
+
+def test_oversized_request_is_rejected_not_queued():
+    sd = syn.default_shell_dict()
+    st = {"numbers": np.array([60] * 200), "positions": np.zeros((200, 3)), "cell": np.eye(3) * 50,
+          "kpoints": np.zeros((1, 3))}
+    server = SV.Server(FakeModel(), sd, device="cpu", mem_budget_bytes=1 << 30, n_workers=1,
+                       executor=lambda s, stream: [{} for _ in s])
+    f = server.submit(st)
+    server.close()
+    assert f.exception() is not None and server.rejected == 1
+
+
+def test_batches_form_from_requests_that_arrive_during_execution():
+    sd = syn.default_shell_dict()
+    sizes = []
+
+    def slow_exec(structures, stream):
+        sizes.append(len(structures))
+        time.sleep(0.05)
+        return [{} for _ in structures]
+
+    server = SV.Server(FakeModel(), sd, device="cpu", mem_budget_bytes=1 << 40, n_workers=1, executor=slow_exec)
+    sts = _structs(20, seed=3)
+    futs = [server.submit(sts[0])]
+    time.sleep(0.01)
+    futs += [server.submit(s) for s in sts[1:]]
+    for f in futs:
+        f.result(timeout=10)
+    server.close()
+    # the first batch holds one request; the rest arrived while it ran and were batched together
+    assert sizes[0] == 1 and max(sizes[1:]) > 1
