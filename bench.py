@@ -48,6 +48,14 @@ WORKLOAD = ("uneven batch: 256 random periodic structures, 2-64 atoms log-unifor
             "1000-pt DOS on [-20,10] eV")
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    sys.stderr.write(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}\n")
+    sys.stderr.flush()
+
+
 def workload(n_struct=N_STRUCT, seed=SEED):
     from slakonet_gb300 import synthetic as syn
     sts = syn.uneven_batch(n_struct, seed=seed)
@@ -189,16 +197,25 @@ def run_gpu(args, rank, world):
     ge.build()
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
+    log("workload")
     sts, tables, sd = workload(args.structures, args.seed)
     model = M.MultiElementSkfParameterOptimizer.from_tables(tables)
     zs = sorted({int(z) for st in sts for z in st["numbers"]})
     ts = model.table_set(sd, dev, zs)
-    eng = E.Engine(ts)
+    from slakonet_gb300 import autotune as AT
     plan = E.plan_batch(sts, ts)
+    log("autotune")
+    t_tune = time.perf_counter()
+    per_bucket = AT.autotune(dev, buckets=AT.buckets_up_to(int(plan.max_n)))   # shape per size bucket (cached)
+    eng = E.Engine(ts)
     db = E.DeviceBatch(plan, dev)
+    tuning = AT.tune_batch(eng, db, AT.candidate_policies(per_bucket))         # policy timed on this batch
+    eng.tuning = tuning
+    t_tune = time.perf_counter() - t_tune
     solves = int(plan.nk.sum())
     flops_eig = float(sum((32.0 / 3.0) * float(n) ** 3 for n in plan.prob_n))
     kw = dict(dos_range=DOS_RANGE, dos_points=DOS_POINTS, dos_sigma=DOS_SIGMA, dos_window=DOS_WINDOW)
+    log("warm-up")
     for _ in range(args.warmup):
         eng.execute(db, **kw)
     torch.cuda.synchronize()
@@ -232,6 +249,7 @@ def run_gpu(args, rank, world):
         elapsed = float(t.item())
     ok = int((res.eig_status == 0).sum().item())
 
+    log("end-to-end")
     # end-to-end through the public batched API from host arrays
     e2e_times, h2d, d2h = [], 0, 0
     barrier()
@@ -253,7 +271,7 @@ def run_gpu(args, rank, world):
         e2e = float(t.item())
 
     peak = fp64_peak(torch, None, dev)
-    eig_t = statistics.mean(per_call["skn_eigh_gen_batched"])
+    eig_t = statistics.mean(per_call["eigensolve"])
     achieved = flops_eig / eig_t / 1e12
     shares = {k: round(sum(v) / elapsed, 4) for k, v in per_call.items()}
     if rank != 0:
@@ -266,8 +284,11 @@ def run_gpu(args, rank, world):
                    "k_point_solves_per_step": solves, "max_n": int(plan.max_n),
                    "mean_n": float(np.mean(plan.prob_n)), "eig_status_ok": ok,
                    "l2": f"inputs larger than L2: H(k)+S(k) {2 * 16 * plan.hs_total / 1e9:.1f} GB per step",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "tensor", "kernel": "k_eigh_gen (skn_eigh_gen_batched)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "eig_launch_shapes": {str(k): (v or "_t128") for k, v in tuning.choice.items()},
+                   "autotune_s": round(t_tune, 1),
+                   "autotune_batch_trials_ms": tuning.timings.get("batch_trials_ms")},
+        "roofline": {"bound": "tensor", "kernel": "k_eigh_gen (skn_eigh_gen_batched, autotuned launch shapes)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": None,
                      "peak_source": "measured in this run: FP64 FMA probe kernel (GB300 FP64 tensor MMA runs at "
@@ -286,6 +307,66 @@ def _single_thread_workers():
     # spawned workers read these at numpy import: one BLAS thread per process
     for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "BLIS_NUM_THREADS"):
         os.environ[v] = "1"
+
+
+def run_training_step(dev, steps=3):
+    """Config-3 fitting step: 64 structures of 4-32 atoms (Z <= 30), DOS MSE + |gap| loss against
+    targets from 5 % perturbed amplitudes (seed 1), hand-written adjoint, AdamW."""
+    import torch
+    from slakonet_gb300 import model as M, synthetic as syn, training as T
+    sts = T.fitting_batch(64, seed=SEED)
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    sd = syn.default_shell_dict()
+    tables = syn.make_tables(zs, sd, seed=SEED)
+    model = M.MultiElementSkfParameterOptimizer.from_tables(tables).to(dev)
+    dos_t, gap_t = T.perturbed_targets(tables, sts, sd, dev, rel=0.05, seed=1)
+    opt = torch.optim.AdamW(model.parameters(), lr=1e-4)
+    T.train_step(model, opt, sts, dos_t, gap_t, sd, dev)           # warm-up
+    rec = [T.train_step(model, opt, sts, dos_t, gap_t, sd, dev) for _ in range(steps)]
+    solves = sum(len(st["kpoints"]) for st in sts)
+    ms = [1e3 * (r["forward_s"] + r["backward_s"]) for r in rec]
+    return {"structures": len(sts), "k_point_solves": solves, "ms_per_step": statistics.median(ms),
+            "forward_ms": 1e3 * statistics.median(r["forward_s"] for r in rec),
+            "backward_ms": 1e3 * statistics.median(r["backward_s"] for r in rec),
+            "loss_first": rec[0]["loss"], "loss_last": rec[-1]["loss"],
+            "degenerate_pairs": rec[-1]["degenerate_pairs"],
+            "note": "forward includes eigenvectors; gradient from the hand-written adjoint (csrc/adjoint.cu)"}
+
+
+def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40):
+    """Config-4-like Poisson stream: 1-200 atoms (log-uniform), Z 1-65, ~1000 k-atoms per structure."""
+    import torch
+    from slakonet_gb300 import model as M, serving as SV, synthetic as syn
+    sts = syn.uneven_batch(n_requests, nmin=1, nmax=200, zmax=65, seed=SEED + 7)
+    for st in sts:
+        st["weights"] = np.full(len(st["kpoints"]), 1.0 / len(st["kpoints"]))
+    sd = syn.default_shell_dict()
+    zs = list(range(1, 66))
+    tables = syn.make_tables(zs, sd, seed=SEED)
+    model = M.MultiElementSkfParameterOptimizer.from_tables(tables)
+    server = SV.Server(model, sd, dev, species=zs, n_workers=3)
+    SV.poisson_stream(server, sts[:8], rate=1000.0, seed=1)          # warm-up
+    lat, wall, res = SV.poisson_stream(server, sts, rate=rate, seed=2)
+    batches = server.batches
+    server.close()
+    # one request at a time through the same API (no batching, no overlap)
+    seq = []
+    for st in sts[:seq_sample]:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = model.compute_properties_batch([st], sd, dev, dos_range=DOS_RANGE, dos_points=DOS_POINTS,
+                                           dos_window=DOS_WINDOW)
+        r.eig.cpu()
+        seq.append(time.perf_counter() - t)
+    nk = [len(st["kpoints"]) for st in sts]
+    return {"requests": n_requests, "rate_per_s": rate, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "structures_per_s": len(lat) / wall,
+            "k_point_solves_per_s": sum(nk) / wall, "batches": batches,
+            "rejected": sum(1 for r in res if "error" in r),
+            "sequential_baseline": {"sample": seq_sample, "p50_ms": 1e3 * float(np.median(seq)),
+                                    "structures_per_s": seq_sample / sum(seq)},
+            "workload": "Poisson arrivals; structures 1-200 atoms log-uniform, Z=1-65, Gamma-centred ~1000 k-atoms; "
+                        "each response: eigenvalues, DOS, gap, Fermi level"}
 
 
 def run_cpu_baseline(sts, tables, sd, reps=1):
@@ -342,6 +423,7 @@ def main():
     ap.add_argument("--structures", type=int, default=N_STRUCT)
     ap.add_argument("--seed", type=int, default=SEED)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the training-step and serving measurements")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -355,8 +437,17 @@ def main():
     r = run_gpu(args, rank, world)
     if rank == 0:
         out, sts, tables, sd = r
+        if world == 1 and not args.no_extras:
+            import torch
+            dev = torch.device("cuda", 0)
+            log("training step")
+            out["training_step"] = run_training_step(dev)
+            log("serving")
+            out["serving"] = run_serving(dev)
         if world == 1 and not args.no_cpu_baseline:
+            log("cpu baseline")
             out["cpu_baseline"] = run_cpu_baseline(sts, tables, sd)
+        log("done")
         print(json.dumps(out))
     if world > 1:
         import torch

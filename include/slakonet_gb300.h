@@ -172,6 +172,30 @@ int skn_eigh_gen_vectors(int n_prob, const int32_t* n, const int64_t* hs_off, co
 int skn_eigh_vectors_scratch_bytes(int n_prob, int max_n, int64_t* bytes);
 
 /*
+ * The same eigensolver compiled in two more launch shapes: 64 threads per CTA
+ * with up to 8 CTAs per SM (suffix _t64), and 256 threads with up to 3 CTAs per
+ * SM (suffix _t256).  The unsuffixed entry points use 128 threads and up to 5
+ * CTAs per SM.  Contracts are identical.  The project's autotuner
+ * (slakonet_gb300/autotune.py) picks a shape per problem-size bucket.
+ */
+int skn_eigh_gen_batched_t64(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                             const int32_t* order, double* H, double* S, double* eig, int32_t* status,
+                             int32_t* work_counter, int max_n, cudaStream_t stream);
+int skn_eigh_gen_batched_t256(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                              const int32_t* order, double* H, double* S, double* eig, int32_t* status,
+                              int32_t* work_counter, int max_n, cudaStream_t stream);
+int skn_eigh_gen_vectors_t64(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                             const int32_t* order, double* H, double* S, double* eig, double* vec, int32_t* status,
+                             double* tri, double* scratch, int64_t scratch_bytes, int32_t* work_counter, int max_n,
+                             cudaStream_t stream);
+int skn_eigh_gen_vectors_t256(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                              const int32_t* order, double* H, double* S, double* eig, double* vec,
+                              int32_t* status, double* tri, double* scratch, int64_t scratch_bytes,
+                              int32_t* work_counter, int max_n, cudaStream_t stream);
+int skn_eigh_vectors_scratch_bytes_t64(int n_prob, int max_n, int64_t* bytes);
+int skn_eigh_vectors_scratch_bytes_t256(int n_prob, int max_n, int64_t* bytes);
+
+/*
  * Fermi level, band gap and band-structure statistics per structure.
  * Replaces fermi_search / fermi_dirac (slakonet/fermi.py:139-215),
  * calculate_band_gap (slakonet/main.py:637-707),
@@ -206,14 +230,15 @@ int skn_dos(int n_struct, const int64_t* eig_off, const int32_t* nk, const int32
  * Adjoint, step 1: weighted eigenvector projectors per problem,
  *   G_ab = sum_n g_n conj(c_n[a]) c_n[b],  F_ab = sum_n g_n e_n conj(c_n[a]) c_n[b],
  * from eigenvectors `vec` (skn_eigh_gen_vectors layout), eigenvalues and
- * grad_eig = dL/de; G, F column-major complex at hs_off[p].  With these,
+ * grad_eig = dL/de; G, F column-major complex at hs_off[p] (zero where
+ * status[p] != SKN_OK; status may be NULL).  With these,
  * dL/dH(k) = G and dL/dS(k) = -F.  Replaces the eigenvalue part of
  * _SymEigB.backward (slakonet/utils.py:387-473), whose complex case omits
  * the conjugate of the eigenvectors.
  */
 int skn_adj_projectors(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
-                       const double* vec, const double* eig, const double* grad_eig, double* G, double* F,
-                       cudaStream_t stream);
+                       const double* vec, const double* eig, const double* grad_eig, const int32_t* status,
+                       double* G, double* F, cudaStream_t stream);
 
 /*
  * Adjoint, step 2: dL/dB for every bond's real-space H and S block,

@@ -44,11 +44,15 @@ SIGNATURES = {
     "skn_fp64_probe": [P, I32, I32, P],
     "skn_eigh_gen_vectors": [I32, P, P, P, P, P, P, P, P, P, P, P, I64, P, I32, P],
     "skn_eigh_vectors_scratch_bytes": [I32, I32, P],
-    "skn_adj_projectors": [I32, P, P, P, P, P, P, P, P, P],
+    "skn_adj_projectors": [I32, P, P, P, P, P, P, P, P, P, P],
     "skn_adj_bloch": [I64] + [P] * 18 + [P],
     "skn_adj_tables": [I64, P, P, P, P, P, P, I32, P, P, P, P, P, P, P, P, P, P, P, P],
     "skn_dos_backward": [I32, P, P, P, P, P, P, P, F64, F64, I32, F64, F64, P, P, I32, P],
 }
+for _sfx in ("_t64", "_t256"):
+    SIGNATURES["skn_eigh_gen_batched" + _sfx] = SIGNATURES["skn_eigh_gen_batched"]
+    SIGNATURES["skn_eigh_gen_vectors" + _sfx] = SIGNATURES["skn_eigh_gen_vectors"]
+    SIGNATURES["skn_eigh_vectors_scratch_bytes" + _sfx] = SIGNATURES["skn_eigh_vectors_scratch_bytes"]
 
 
 class SknError(RuntimeError):

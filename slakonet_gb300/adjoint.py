@@ -83,8 +83,9 @@ def adjoint(eng: "E.Engine", res: "E.BatchResult", g_eig=None, g_dos=None, g_gap
     Gm = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
     Fm = torch.empty_like(Gm)
     vec = torch.view_as_real(res.vec).reshape(-1)
+    g = torch.nan_to_num(g, nan=0.0, posinf=0.0, neginf=0.0)
     call("skn_adj_projectors", n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(vec), ptr(res.eig), ptr(g),
-         ptr(Gm), ptr(Fm), stream)
+         ptr(res.eig_status), ptr(Gm), ptr(Fm), stream)
     nbond = st["nbond"]
     dtab_H = torch.zeros_like(T.tab_H)
     dtab_S = torch.zeros_like(T.tab_S)

@@ -20,6 +20,9 @@ BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libslakonet_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# Extra launch shapes of the eigensolver, exported with a suffix and chosen per problem-size
+# bucket by slakonet_gb300.autotune: (suffix, threads per CTA, CTAs per SM, unroll, shared-memory staging n).
+EIG_SHAPES = [("_t64", 64, 8, 2, 16), ("_t256", 256, 3, 2, 32)]
 
 
 def nvcc() -> str:
@@ -48,9 +51,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cc = nvcc()
     inc = ["-I", os.path.join(ROOT, "include")]
 
-    def compile_one(src):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [cc, *ARCH, *FLAGS, *inc, "-c", src, "-o", obj]
+    def compile_one(job):
+        src, extra, tag = job
+        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + tag + ".o")
+        cmd = [cc, *ARCH, *FLAGS, *inc, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")
@@ -58,8 +62,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(r.stderr)
         return obj
 
+    jobs = [(src, [], "") for src in sources()]
+    eig = os.path.join(CSRC, "eigh.cu")
+    for suffix, nt, minb, unr, smem_n in EIG_SHAPES:
+        jobs.append((eig, [f"-DSKN_EIG_SUFFIX={suffix}", f"-DSKN_EIG_NT={nt}", f"-DSKN_EIG_MINB={minb}",
+                           f"-DSKN_EIG_UNR={unr}", f"-DSKN_EIG_SMEM_N={smem_n}"], suffix))
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
-        objs = list(ex.map(compile_one, sources()))
+        objs = list(ex.map(compile_one, jobs))
     tmp = LIB + ".tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -28,8 +28,8 @@ __global__ void __launch_bounds__(256) k_adj_projectors(int n_prob, const int32_
                                                         const int64_t* __restrict__ hs_off,
                                                         const int64_t* __restrict__ eig_off,
                                                         const double2* __restrict__ C, const double* __restrict__ eig,
-                                                        const double* __restrict__ g, double2* __restrict__ G,
-                                                        double2* __restrict__ F) {
+                                                        const double* __restrict__ g, const int32_t* __restrict__ status,
+                                                        double2* __restrict__ G, double2* __restrict__ F) {
   __shared__ double2 ca[16][17], cb[16][17];
   __shared__ double gj[16], gej[16];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -40,6 +40,13 @@ __global__ void __launch_bounds__(256) k_adj_projectors(int n_prob, const int32_
     const double* gp = g + eig_off[p];
     double2* Gp = G + hs_off[p];
     double2* Fp = F + hs_off[p];
+    if (status != nullptr && status[p] != SKN_OK) {   // failed problem: NaN vectors carry no gradient
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        Gp[e] = make_double2(0.0, 0.0);
+        Fp[e] = make_double2(0.0, 0.0);
+      }
+      continue;
+    }
     for (int a0 = 0; a0 < n; a0 += 16) {
       for (int b0 = 0; b0 < n; b0 += 16) {
         const int a = a0 + tx, b = b0 + ty;
@@ -252,14 +259,14 @@ __global__ void __launch_bounds__(256) k_dos_backward(const int64_t* __restrict_
 }  // namespace
 
 extern "C" int skn_adj_projectors(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
-                                  const double* vec, const double* eig, const double* grad_eig, double* G, double* F,
-                                  cudaStream_t stream) {
+                                  const double* vec, const double* eig, const double* grad_eig,
+                                  const int32_t* status, double* G, double* F, cudaStream_t stream) {
   if (n_prob < 0) return SKN_ERR_ARG;
   if (n_prob == 0) return SKN_OK;
   if (!n || !hs_off || !eig_off || !vec || !eig || !grad_eig || !G || !F) return SKN_ERR_ARG;
   const int grid = n_prob < 152 * 8 ? n_prob : 152 * 8;
   k_adj_projectors<<<grid, 256, 0, stream>>>(n_prob, n, hs_off, eig_off, (const double2*)vec, eig, grad_eig,
-                                             (double2*)G, (double2*)F);
+                                             status, (double2*)G, (double2*)F);
   return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
 }
 

@@ -35,10 +35,22 @@ namespace {
 #ifndef SKN_EIG_SMEM_N
 #define SKN_EIG_SMEM_N 24
 #endif
+// Exported names carry SKN_EIG_SUFFIX so several launch shapes can live in one library.
+#ifndef SKN_EIG_SUFFIX
+#define SKN_EIG_SUFFIX
+#endif
+#define SKN_CAT2(a, b) a##b
+#define SKN_CAT(a, b) SKN_CAT2(a, b)
+#define SKN_EXPORT(name) SKN_CAT(name, SKN_EIG_SUFFIX)
 constexpr int NT = SKN_EIG_NT;    // threads per CTA
 constexpr int NW = NT / 32;
 constexpr int SMEM_N = SKN_EIG_SMEM_N;   // problems up to this size run from shared memory
 constexpr int SMEM_LDA = SMEM_N + 1;
+// The shared-memory region stages small problems (H and S, 2*SMEM_LDA*SMEM_N elements) and,
+// for problems solved in global memory, holds the 32x33 tile of the triangular solve.
+constexpr int TILE_ELEMS = 32 * 33;
+constexpr int SMEM_REGION = (2 * SMEM_LDA * SMEM_N > TILE_ELEMS) ? 2 * SMEM_LDA * SMEM_N : TILE_ELEMS;
+static_assert(SMEM_REGION >= TILE_ELEMS && SMEM_REGION >= 2 * SMEM_LDA * SMEM_N, "staging region too small");
 constexpr int MAX_N = 2048;       // shared-memory vectors bound the single-CTA path
 
 struct Vecs {
@@ -862,7 +874,7 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
 // from several host threads never lower the limit under another's launch.
 static size_t eig_smem_bytes(int mn) {
   return sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn) +
-         2 * SMEM_LDA * SMEM_N * sizeof(double2);
+         SMEM_REGION * sizeof(double2);
 }
 static size_t vec_smem_bytes(int mn) {
   return sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;
@@ -874,7 +886,7 @@ static cudaError_t set_smem_limit_once() {
   return cudaFuncSetAttribute(k_eigvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_smem_bytes(MAX_N));
 }
 
-extern "C" int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+extern "C" int SKN_EXPORT(skn_eigh_gen_batched)(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
                                     const int32_t* order, double* H, double* S, double* eig, int32_t* status,
                                     int32_t* work_counter, int max_n, cudaStream_t stream) {
   if (n_prob < 0 || max_n < 0) return SKN_ERR_ARG;
@@ -884,7 +896,7 @@ extern "C" int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t*
   const int mn = max_n < 1 ? 1 : max_n;
   const int use_smem_mats = 1;
   size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn);
-  smem += (size_t)use_smem_mats * 2 * SMEM_LDA * SMEM_N * sizeof(double2);
+  smem += (size_t)use_smem_mats * SMEM_REGION * sizeof(double2);
   if (set_smem_limit_once() != cudaSuccess) return SKN_ERR_CUDA;
   int per_sm = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -907,13 +919,13 @@ static int vec_grid(int n_prob) {
   return g < n_prob ? g : (n_prob > 0 ? n_prob : 1);
 }
 
-extern "C" int skn_eigh_vectors_scratch_bytes(int n_prob, int max_n, int64_t* bytes) {
+extern "C" int SKN_EXPORT(skn_eigh_vectors_scratch_bytes)(int n_prob, int max_n, int64_t* bytes) {
   if (!bytes || max_n < 0 || n_prob < 0) return SKN_ERR_ARG;
   *bytes = (int64_t)vec_grid(n_prob) * 5 * (int64_t)(max_n < 1 ? 1 : max_n) * VNT * (int64_t)sizeof(double);
   return SKN_OK;
 }
 
-extern "C" int skn_eigh_gen_vectors(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+extern "C" int SKN_EXPORT(skn_eigh_gen_vectors)(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
                                     const int32_t* order, double* H, double* S, double* eig, double* vec,
                                     int32_t* status, double* tri, double* scratch, int64_t scratch_bytes,
                                     int32_t* work_counter, int max_n, cudaStream_t stream) {
@@ -924,12 +936,12 @@ extern "C" int skn_eigh_gen_vectors(int n_prob, const int32_t* n, const int64_t*
     return SKN_ERR_ARG;
   if (max_n > MAX_N) return SKN_ERR_CAPACITY;
   int64_t need = 0;
-  skn_eigh_vectors_scratch_bytes(n_prob, max_n, &need);
+  SKN_EXPORT(skn_eigh_vectors_scratch_bytes)(n_prob, max_n, &need);
   if (scratch_bytes < need) return SKN_ERR_CAPACITY;
   const int mn = max_n < 1 ? 1 : max_n;
   const int use_smem_mats = 1;
   size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn);
-  smem += (size_t)use_smem_mats * 2 * SMEM_LDA * SMEM_N * sizeof(double2);
+  smem += (size_t)use_smem_mats * SMEM_REGION * sizeof(double2);
   if (set_smem_limit_once() != cudaSuccess) return SKN_ERR_CUDA;
   int per_sm = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);

@@ -344,9 +344,11 @@ KERNELS_PER_CALL = {"skn_bond_counts": 1, "skn_bond_fill": 1, "skn_image_phases"
 class Engine:
     """Runs the whole path for a planned batch on one CUDA stream."""
 
-    def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None):
+    def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None,
+                 tuning=None):
         _dev(tables.device)
         self.tables = tables
+        self.tuning = tuning          # autotune.Tuning: eigensolver launch shape per problem-size bucket
         self.cutoff = float(cutoff)
         self.device = tables.device
         self.stream = stream
@@ -378,15 +380,21 @@ class Engine:
                 dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False,
                 vectors: bool = False, keep_state: bool = False) -> BatchResult:
         """Kernels only, on the current stream; one device->host read sizes the bond table."""
+        bonds = self.bonds(db)
+        return self.tail(db, bonds, dos_range, dos_points, dos_sigma, dos_window, keep_hs, hs_only, vectors,
+                         keep_state)
+
+    def bonds(self, db: DeviceBatch) -> dict:
+        """Neighbour list: counts, host scan (one device->host read), fill.  The result is the
+        structure-only part of the path and stays valid while the geometry does."""
         plan = db.plan
         dev = self.device
-        T = self.tables
         S = plan.n_struct
         stream = torch.cuda.current_stream(dev).cuda_stream
         counts = torch.empty(max(plan.n_pairs, 1), dtype=torch.int32, device=dev)
         self._call("skn_bond_counts", S, plan.n_pairs, ptr(db.atom_ptr), ptr(db.pos), ptr(db.cells), ptr(db.rng),
                    self.cutoff, ptr(db.pair_base), ptr(counts), stream)
-        cnt = counts[: plan.n_pairs].to("cpu").numpy().astype(np.int64)   # sizes the bond table (one sync)
+        cnt = counts[: plan.n_pairs].to("cpu").numpy().astype(np.int64)
         pair_ptr = np.zeros(plan.n_pairs + 1, np.int64)
         np.cumsum(cnt, out=pair_ptr[1:])
         pair_blk = np.zeros(plan.n_pairs + 1, np.int64)
@@ -396,15 +404,33 @@ class Engine:
         d_pair_ptr = _i64(pair_ptr, dev)
         d_pair_blk = _i64(pair_blk[:-1] if plan.n_pairs else np.zeros(1), dev)
         nb1 = max(nbond, 1)
-        bond_i = torch.empty(nb1, dtype=torch.int32, device=dev)
-        bond_j = torch.empty(nb1, dtype=torch.int32, device=dev)
-        bond_img = torch.empty(nb1, dtype=torch.int32, device=dev)
-        bond_d = torch.empty(nb1, dtype=torch.float64, device=dev)
-        bond_u = torch.empty(3 * nb1, dtype=torch.float64, device=dev)
-        bond_blk = torch.empty(nb1, dtype=torch.int64, device=dev)
+        b = dict(nbond=nbond, nblk=nblk, pair_ptr=d_pair_ptr,
+                 bond_i=torch.empty(nb1, dtype=torch.int32, device=dev),
+                 bond_j=torch.empty(nb1, dtype=torch.int32, device=dev),
+                 bond_img=torch.empty(nb1, dtype=torch.int32, device=dev),
+                 bond_d=torch.empty(nb1, dtype=torch.float64, device=dev),
+                 bond_u=torch.empty(3 * nb1, dtype=torch.float64, device=dev),
+                 bond_blk=torch.empty(nb1, dtype=torch.int64, device=dev))
         self._call("skn_bond_fill", S, plan.n_pairs, ptr(db.atom_ptr), ptr(db.pos), ptr(db.cells), ptr(db.rng),
-                   self.cutoff, ptr(db.pair_base), ptr(d_pair_ptr), ptr(d_pair_blk), ptr(db.norb), ptr(bond_i),
-                   ptr(bond_j), ptr(bond_img), ptr(bond_d), ptr(bond_u), ptr(bond_blk), stream)
+                   self.cutoff, ptr(db.pair_base), ptr(d_pair_ptr), ptr(d_pair_blk), ptr(db.norb), ptr(b["bond_i"]),
+                   ptr(b["bond_j"]), ptr(b["bond_img"]), ptr(b["bond_d"]), ptr(b["bond_u"]), ptr(b["bond_blk"]),
+                   stream)
+        return b
+
+    def tail(self, db: DeviceBatch, bonds: dict, dos_range=(-10.0, 10.0), dos_points: int = 5000,
+             dos_sigma: float = 0.1, dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False,
+             vectors: bool = False, keep_state: bool = False) -> BatchResult:
+        """Everything after the neighbour list; device work only (no host synchronisation), so
+        it can be captured in a CUDA graph."""
+        plan = db.plan
+        dev = self.device
+        T = self.tables
+        S = plan.n_struct
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        nbond, nblk = bonds["nbond"], bonds["nblk"]
+        bond_i, bond_j, bond_img = bonds["bond_i"], bonds["bond_j"], bonds["bond_img"]
+        bond_d, bond_u, bond_blk = bonds["bond_d"], bonds["bond_u"], bonds["bond_blk"]
+        d_pair_ptr = bonds["pair_ptr"]
         phases = torch.empty(2 * max(plan.n_phase, 1), dtype=torch.float64, device=dev)
         self._call("skn_image_phases", S, ptr(db.rng), ptr(db.kptr), ptr(db.kp), ptr(db.phb), ptr(phases), stream)
         blk_H = torch.empty(max(nblk, 1), dtype=torch.float64, device=dev)
@@ -442,8 +468,17 @@ class Engine:
                        int(need.value), ptr(counter), plan.max_n, stream)
             vec = torch.view_as_complex(vec.view(-1, 2))
         else:
-            self._call("skn_eigh_gen_batched", n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order),
-                       ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counter), plan.max_n, stream)
+            ev = self.event_log
+            if ev is not None:
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record()
+                self.event_log = None        # the phase is timed as a whole (groups run on forked streams)
+            self._eig_values(db, Hk, Sk, eig, eig_status, counter, stream)
+            if ev is not None:
+                b.record()
+                self.event_log = ev
+                ev.append(("eigensolve", a, b))
         mu = torch.empty(S, dtype=torch.float64, device=dev)
         stats = torch.zeros(S * _lib.SKN_NSTAT, dtype=torch.float64, device=dev)
         fst = torch.empty(S, dtype=torch.int32, device=dev)
@@ -463,10 +498,106 @@ class Engine:
                                        float(dos_window)))
         return out
 
+    def _eig_values(self, db, Hk, Sk, eig, eig_status, counter, stream):
+        plan = db.plan
+        n_prob = len(plan.prob_n)
+        groups = self._groups(db)
+        if len(groups) <= 1:
+            sfx = groups[0][0] if groups else ""
+            self._call("skn_eigh_gen_batched" + sfx, n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order),
+                       ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counter), plan.max_n, stream)
+            return
+        # one launch per shape, largest problems' group first, on forked streams
+        main = torch.cuda.current_stream(self.device)
+        fork = torch.cuda.Event()
+        fork.record(main)
+        joins = []
+        counters = torch.zeros(2 * len(groups), dtype=torch.int32, device=self.device)
+        for gi, (sfx, order_g, count, max_n) in enumerate(groups):
+            st = self._side_streams(len(groups))[gi]
+            st.wait_event(fork)
+            with torch.cuda.stream(st):
+                self._call("skn_eigh_gen_batched" + sfx, count, ptr(db.n), ptr(db.hs_off), ptr(db.eoff),
+                           ptr(order_g), ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counters[2 * gi:]),
+                           max_n, st.cuda_stream)
+            ev = torch.cuda.Event()
+            ev.record(st)
+            joins.append(ev)
+        for ev in joins:
+            main.wait_event(ev)
+
+    def _side_streams(self, k):
+        cur = getattr(self, "_sides", [])
+        while len(cur) < k:
+            cur.append(torch.cuda.Stream(self.device))
+        self._sides = cur
+        return cur
+
+    def _groups(self, db):
+        """[(suffix, device order, count, max_n)] for the tuning, cached on the batch."""
+        if self.tuning is None:
+            return []
+        key = id(self.tuning)
+        cache = getattr(db, "_groups", None)
+        if cache is not None and cache[0] == key:
+            return cache[1]
+        plan = db.plan
+        shapes = np.array([self.tuning.shape_for(int(n)) for n in plan.prob_n[plan.order]])
+        out = []
+        for sfx in dict.fromkeys(shapes.tolist()):
+            sel = plan.order[shapes == sfx]
+            out.append((sfx, _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))
+        db._groups = (key, out)
+        return out
+
     def check_tables(self):
         """Raise if the last execute() needed a table the parameter set lacks (reads one device int)."""
         if int(self._status.item()) != 0:
             raise _lib.SknError("sk_blocks: a Slater-Koster table needed by this structure is missing")
+
+
+class CapturedPath:
+    """A batch whose geometry is fixed: the neighbour list is built once and kept on the
+    device, and the rest of the path is captured in a CUDA graph.
+
+    ``replay()`` re-runs phases, SK blocks, Bloch sums, eigensolve, Fermi/gap
+    and DOS with no host work; it reads the tables from the ``TableSet``
+    buffers, so writing new parameter values into ``tables.tab_H`` /
+    ``tab_S`` in place (``refresh_tables``) and replaying evaluates the new
+    parameters.  Outputs live in ``self.result`` (fixed addresses).
+    """
+
+    def __init__(self, engine: "Engine", db: DeviceBatch, **tail_kw):
+        self.engine = engine
+        self.db = db
+        dev = engine.device
+        self.bonds = engine.bonds(db)
+        torch.cuda.synchronize(dev)
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            engine.tail(db, self.bonds, **tail_kw)          # warm-up outside the graph
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        launches = engine.launches
+        with torch.cuda.graph(self.graph, capture_error_mode="thread_local"):
+            self.result = engine.tail(db, self.bonds, **tail_kw)
+        self.kernels_per_replay = engine.launches - launches
+        self.graph.replay()              # the capture itself runs nothing; fill the outputs once
+        torch.cuda.synchronize(dev)
+        engine.check_tables()
+
+    def replay(self) -> "BatchResult":
+        self.graph.replay()
+        self.engine.launches += self.kernels_per_replay
+        return self.result
+
+    def refresh_tables(self, tables: "TableSet"):
+        """Copy new table values into the captured buffers (same packing)."""
+        T = self.engine.tables
+        T.tab_H.copy_(tables.tab_H)
+        T.tab_S.copy_(tables.tab_S)
 
 
 class _nullctx:

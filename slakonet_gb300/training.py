@@ -57,12 +57,26 @@ def train_step(model: MultiElementSkfParameterOptimizer, optimizer: torch.optim.
     per = dos_weight * ((dos - dos_target) ** 2).mean(1) + gap_weight * (gap - gap_target).abs()
     w = torch.as_tensor(np.diff(res.plan.atom_ptr).astype(np.float64) if weight_by_natoms
                         else np.ones(res.plan.n_struct), device=per.device)
-    batch_loss = (per * w).sum() / w.sum()
-    reg = sum((p.to(per.device) ** 2).sum() for p in model.parameters())
-    loss = batch_loss + 1e-10 * reg
+    # a structure whose Fermi search diverged (NaN, as in the reference) or whose S(k) is not
+    # positive definite drops out of the batch; the reference skips the whole step instead
+    ok = torch.isfinite(per) & torch.isfinite(dos_target).all(1) & torch.isfinite(gap_target)
+    per = torch.where(ok, per, torch.zeros_like(per))
+    w = torch.where(ok, w, torch.zeros_like(w))
+    batch_loss = (per * w).sum() / w.sum().clamp(min=1e-300)
+    params = [p for p in model.parameters()]
+    # 1e-10 * sum(theta^2): value from fused norms, gradient 2e-10 * theta added after backward
+    with torch.no_grad():
+        reg = float(torch.stack(torch._foreach_norm(params)).pow(2).sum())
     t1 = time.perf_counter()
-    loss.backward()
-    torch.nn.utils.clip_grad_norm_(model.parameters(), max_norm=clip)
+    batch_loss.backward()
+    with torch.no_grad():
+        grads = [p.grad if p.grad is not None else torch.zeros_like(p) for p in params]
+        for p, gr in zip(params, grads):
+            if p.grad is None:
+                p.grad = gr
+        torch._foreach_add_(grads, params, alpha=2e-10)
+    loss = batch_loss.detach() + 1e-10 * reg
+    torch.nn.utils.clip_grad_norm_(params, max_norm=clip)
     optimizer.step()
     if scheduler is not None:
         scheduler.step(loss.detach())
@@ -71,4 +85,5 @@ def train_step(model: MultiElementSkfParameterOptimizer, optimizer: torch.optim.
     t2 = time.perf_counter()
     st = res.state or {}
     return {"loss": float(loss.detach()), "batch_loss": float(batch_loss.detach()), "forward_s": t1 - t0,
+            "structures_used": int(ok.sum()),
             "backward_s": t2 - t1, "degenerate_pairs": int(st.get("degenerate_pairs", 0))}
