@@ -172,6 +172,33 @@ int skn_eigh_gen_vectors(int n_prob, const int32_t* n, const int64_t* hs_off, co
 int skn_eigh_vectors_scratch_bytes(int n_prob, int max_n, int64_t* bytes);
 
 /*
+ * skn_eigh_gen_vectors without any device allocation: no counterpart in the
+ * reference (which allocates through torch on every call).  For callers that
+ * cannot allocate device memory: a host binding that receives only device
+ * pointers from another runtime and owns no allocator, or a latency-bound
+ * service that keeps cudaMalloc/cudaFree (which can synchronise the device or
+ * fail under memory pressure) out of its request path.
+ * Same outputs, same contract, minus tri, scratch and work_counter: those live
+ * in one fixed library-owned device array (about 40 MiB per device, reserved
+ * when the library's module is loaded on that device).
+ *   n_rows   length of eig = sum of n[p] (every eig_off[p] + n[p] <= n_rows)
+ * Limits: max_n <= SKN_NOALLOC_MAX_N and n_rows <= SKN_NOALLOC_MAX_ROWS, else
+ * SKN_ERR_CAPACITY and nothing is launched.  The vector stage runs on as many
+ * CTAs as the fixed workspace holds (up to 2 per SM), so large batches are
+ * slower than with skn_eigh_gen_vectors.
+ * The first call on a device looks up the array's address on the current
+ * device; make it before any stream capture.  Calls share the array: two
+ * calls in flight at once on one device (other streams or host threads) race
+ * and corrupt each other; order them on one stream or serialise them.
+ */
+#define SKN_NOALLOC_MAX_N 512
+#define SKN_NOALLOC_MAX_ROWS 262144             /* 8 MiB of tridiagonal rows            */
+#define SKN_NOALLOC_SCRATCH_DOUBLES 4194304     /* 32 MiB of inverse-iteration scratch  */
+int skn_eigh_gen_vectors_noalloc(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                                 const int32_t* order, double* H, double* S, double* eig, double* vec,
+                                 int32_t* status, int64_t n_rows, int max_n, cudaStream_t stream);
+
+/*
  * The same eigensolver compiled in two more launch shapes: 64 threads per CTA
  * with up to 8 CTAs per SM (suffix _t64), and 256 threads with up to 3 CTAs per
  * SM (suffix _t256).  The unsuffixed entry points use 128 threads and up to 5

@@ -886,6 +886,9 @@ static cudaError_t set_smem_limit_once() {
   return cudaFuncSetAttribute(k_eigvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_smem_bytes(MAX_N));
 }
 
+// A translation unit that includes this file for its kernels alone defines
+// SKN_EIG_KERNELS_ONLY and provides its own entry points.
+#ifndef SKN_EIG_KERNELS_ONLY
 extern "C" int SKN_EXPORT(skn_eigh_gen_batched)(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
                                     const int32_t* order, double* H, double* S, double* eig, int32_t* status,
                                     int32_t* work_counter, int max_n, cudaStream_t stream) {
@@ -961,3 +964,4 @@ extern "C" int SKN_EXPORT(skn_eigh_gen_vectors)(int n_prob, const int32_t* n, co
                                                      work_counter + 1, mn);
   return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
 }
+#endif  // SKN_EIG_KERNELS_ONLY
