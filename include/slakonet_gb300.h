@@ -199,6 +199,26 @@ int skn_eigh_gen_vectors_noalloc(int n_prob, const int32_t* n, const int64_t* hs
                                  int32_t* status, int64_t n_rows, int max_n, cudaStream_t stream);
 
 /*
+ * Eigenvalues of large problems, one thread-block cluster per problem.
+ * Replaces the same eighb call as skn_eigh_gen_batched (slakonet/utils.py:
+ * 741-783) for problems that are too slow on one SM or too large for its
+ * shared memory (n > 2048).  Same steps, results to rounding: `cluster` CTAs
+ * (1..16, one per SM) split every O(n^2)-per-column loop of the Cholesky,
+ * reduction and tridiagonalisation and the bisection, with cluster barriers
+ * between phases.  Arguments as skn_eigh_gen_batched, plus
+ *   scratch   device scratch of skn_eigh_large_scratch_bytes(n_prob, max_n, cluster) bytes
+ *   cluster   CTAs per problem (more than 8 uses the non-portable cluster size)
+ * max_n <= 9216 (the tridiagonal is bisected from shared memory), else
+ * SKN_ERR_CAPACITY; SKN_ERR_CAPACITY also when no cluster of that size fits.
+ */
+int skn_eigh_gen_large(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                       const int32_t* order, double* H, double* S, double* eig, int32_t* status,
+                       int32_t* work_counter, double* scratch, int64_t scratch_bytes, int max_n, int cluster,
+                       cudaStream_t stream);
+/* Host-side query: bytes of `scratch` skn_eigh_gen_large needs (written to *bytes). */
+int skn_eigh_large_scratch_bytes(int n_prob, int max_n, int cluster, int64_t* bytes);
+
+/*
  * The same eigensolver compiled in two more launch shapes: 64 threads per CTA
  * with up to 8 CTAs per SM (suffix _t64), and 256 threads with up to 3 CTAs per
  * SM (suffix _t256).  The unsuffixed entry points use 128 threads and up to 5

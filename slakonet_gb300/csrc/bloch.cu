@@ -1,6 +1,8 @@
 // Bloch sums: H(k) = onsite + sum_T H(T) exp(i 2 pi k.T), and S(k) alike.
 //
-// One CTA per (structure, k) problem; each warp takes ordered atom pairs
+// CTAs stride over (structure, k) problems (blockIdx.x) and, for batches with
+// fewer problems than the GPU has CTA slots, split each problem's atom pairs
+// (blockIdx.y); each warp takes ordered atom pairs
 // (i, j) and its lanes take the elements of the norb_i x norb_j block, so a
 // warp walks one bond list with uniform trip count: every lane reads the same
 // bond index and phase (broadcast) and its own block element (contiguous).
@@ -31,7 +33,7 @@ __global__ void __launch_bounds__(256) k_bloch(
     double2* Hp = H + hs_off[p];
     double2* Sp = S + hs_off[p];
     const int64_t pb = pair_base[s];
-    for (int q = wib; q < N * N; q += nw) {
+    for (int q = blockIdx.y * nw + wib; q < N * N; q += nw * gridDim.y) {
       const int ib = q / N, ia = q % N;  // consecutive warps: consecutive row blocks of one column block
       const int gi = a0 + ia, gj = a0 + ib;
       const int ni = atom_norb[gi], nj = atom_norb[gj];
@@ -71,14 +73,24 @@ extern "C" int skn_bloch(int n_prob, const int32_t* prob_struct, const int32_t* 
                          const int64_t* phase_base, const double* phases, const double* onsite_H,
                          int max_n, double* H, double* S, cudaStream_t stream) {
   (void)orb_atom;
-  (void)max_n;
   if (n_prob < 0) return SKN_ERR_ARG;
   if (n_prob == 0) return SKN_OK;
   if (!prob_struct || !prob_k || !hs_off || !atom_ptr || !orb_ptr || !atom_orb_off || !atom_norb || !pair_base ||
       !pair_ptr || !image_range || !phase_base || !phases || !onsite_H || !H || !S)
     return SKN_ERR_ARG;
-  int blocks = n_prob < 152 * 8 ? n_prob : 152 * 8;
-  k_bloch<<<blocks, 256, 0, stream>>>(n_prob, prob_struct, prob_k, hs_off, atom_ptr, orb_ptr, atom_orb_off, atom_norb,
+  if (max_n < 0) return SKN_ERR_ARG;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int slots = 8 * (sms > 0 ? sms : 1);          // 256-thread CTAs resident at once
+  const int bx = n_prob < slots ? n_prob : slots;
+  // split problems over blockIdx.y only as far as there are warps of atom pairs to give out
+  const int64_t pair_warps = ((int64_t)max_n * max_n + 7) / 8;
+  int64_t by = (slots + bx - 1) / bx;
+  if (by > pair_warps) by = pair_warps;
+  if (by < 1) by = 1;
+  if (by > 65535) by = 65535;
+  k_bloch<<<dim3(bx, (unsigned)by), 256, 0, stream>>>(n_prob, prob_struct, prob_k, hs_off, atom_ptr, orb_ptr, atom_orb_off, atom_norb,
                                       pair_base, pair_ptr, bond_img, bond_blk, blk_H, blk_S, image_range, phase_base,
                                       (const double2*)phases, onsite_H, (double2*)H, (double2*)S);
   return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;

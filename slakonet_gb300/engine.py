@@ -338,17 +338,51 @@ class DeviceBatch:
 # kernels each ABI call launches (for the launch count the bench reports)
 KERNELS_PER_CALL = {"skn_bond_counts": 1, "skn_bond_fill": 1, "skn_image_phases": 1, "skn_sk_blocks": 1,
                     "skn_bloch": 1, "skn_eigh_gen_batched": 1, "skn_eigh_gen_vectors": 2, "skn_fermi_gap": 1,
-                    "skn_dos": 2}
+                    "skn_dos": 2, "skn_eigh_gen_large": 1, "skn_eigh_gen_vectors_noalloc": 2}
+
+SINGLE_CTA_MAX_N = 2048   # bound of the one-CTA-per-problem eigensolver (csrc/eigh.cu)
+LARGE_MAX_N = 9216        # bound of the cluster eigensolver (csrc/eigh_cluster.cu)
+
+
+def cluster_for(n: int) -> int:
+    """CTAs (SMs) the cluster eigensolver gives one problem of n orbitals.
+
+    Measured on GB300 (one problem alone, random Hermitian-definite pairs): at n = 1024
+    one SM takes 3.6 s, clusters of 2/4/8/16 CTAs 1.27/1.03/0.91/0.86 s; at n = 2048 one
+    SM takes 27 s and clusters 8.0/5.2/4.3/3.8 s.  Four CTAs keep most of the gain up to
+    2048 while 38 problems still run at once; larger problems get 8, then 16."""
+    return 4 if n <= 2048 else (8 if n <= 4096 else 16)
+
+
+def route_large(prob_n: np.ndarray, threshold: Optional[int] = 1024, cluster: Optional[int] = None) -> np.ndarray:
+    """Cluster size per problem, 0 for the one-CTA-per-problem eigensolver.
+
+    Problems above ``threshold`` orbitals (and always those above SINGLE_CTA_MAX_N) go to
+    the cluster eigensolver with ``cluster`` CTAs, or ``cluster_for(n)`` when it is None.
+    The choice depends on each problem alone, never on the rest of the batch, so a
+    structure's results are bitwise the same whatever it is batched with."""
+    n = prob_n.astype(np.int64)
+    mask = n > SINGLE_CTA_MAX_N
+    if threshold is not None:
+        mask |= n > int(threshold)
+    sizes = np.zeros(len(n), dtype=np.int64)
+    for i in np.nonzero(mask)[0]:
+        sizes[i] = cluster if cluster is not None else cluster_for(int(n[i]))
+    return sizes
 
 
 class Engine:
     """Runs the whole path for a planned batch on one CUDA stream."""
 
     def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None,
-                 tuning=None):
+                 tuning=None, large_threshold: Optional[int] = 1024, large_cluster: Optional[int] = None):
         _dev(tables.device)
         self.tables = tables
         self.tuning = tuning          # autotune.Tuning: eigensolver launch shape per problem-size bucket
+        # which problems run on the cluster eigensolver and with how many CTAs (SMs) each:
+        # see route_large (large_cluster None: cluster_for(n))
+        self.large_threshold = large_threshold
+        self.large_cluster = large_cluster
         self.cutoff = float(cutoff)
         self.device = tables.device
         self.stream = stream
@@ -502,24 +536,41 @@ class Engine:
         plan = db.plan
         n_prob = len(plan.prob_n)
         groups = self._groups(db)
-        if len(groups) <= 1:
-            sfx = groups[0][0] if groups else ""
-            self._call("skn_eigh_gen_batched" + sfx, n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order),
+        if not groups:
+            self._call("skn_eigh_gen_batched", n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order),
                        ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counter), plan.max_n, stream)
             return
-        # one launch per shape, largest problems' group first, on forked streams
+        scratch = {}
+        for gi, (shape, _, count, max_n) in enumerate(groups):
+            if isinstance(shape, int):       # a cluster group
+                need = ctypes.c_int64(0)
+                call("skn_eigh_large_scratch_bytes", count, max_n, shape, ctypes.addressof(need))
+                scratch[gi] = torch.empty(max(need.value // 8, 1), dtype=torch.float64, device=self.device)
+        counters = torch.zeros(2 * len(groups), dtype=torch.int32, device=self.device)
+
+        def launch(gi, sfx, order_g, count, max_n, st):
+            if isinstance(sfx, int):
+                self._call("skn_eigh_gen_large", count, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(order_g),
+                           ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counters[2 * gi:]), ptr(scratch[gi]),
+                           int(scratch[gi].numel() * 8), max_n, sfx, st)
+            else:
+                self._call("skn_eigh_gen_batched" + sfx, count, ptr(db.n), ptr(db.hs_off), ptr(db.eoff),
+                           ptr(order_g), ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counters[2 * gi:]),
+                           max_n, st)
+
+        if len(groups) == 1:
+            launch(0, *groups[0], stream)
+            return
+        # one launch per group (cluster group first, then shapes by problem size) on forked streams
         main = torch.cuda.current_stream(self.device)
         fork = torch.cuda.Event()
         fork.record(main)
         joins = []
-        counters = torch.zeros(2 * len(groups), dtype=torch.int32, device=self.device)
-        for gi, (sfx, order_g, count, max_n) in enumerate(groups):
+        for gi, g in enumerate(groups):
             st = self._side_streams(len(groups))[gi]
             st.wait_event(fork)
             with torch.cuda.stream(st):
-                self._call("skn_eigh_gen_batched" + sfx, count, ptr(db.n), ptr(db.hs_off), ptr(db.eoff),
-                           ptr(order_g), ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counters[2 * gi:]),
-                           max_n, st.cuda_stream)
+                launch(gi, *g, st.cuda_stream)
             ev = torch.cuda.Event()
             ev.record(st)
             joins.append(ev)
@@ -534,19 +585,32 @@ class Engine:
         return cur
 
     def _groups(self, db):
-        """[(suffix, device order, count, max_n)] for the tuning, cached on the batch."""
-        if self.tuning is None:
-            return []
-        key = id(self.tuning)
+        """[(launch shape suffix, or the cluster size for the cluster path, device order, count, max_n)],
+        cached on the batch.
+
+        Empty when every problem takes the default single-CTA launch."""
+        plan = db.plan
+        key = (id(self.tuning), self.large_threshold, self.large_cluster)
         cache = getattr(db, "_groups", None)
         if cache is not None and cache[0] == key:
             return cache[1]
-        plan = db.plan
-        shapes = np.array([self.tuning.shape_for(int(n)) for n in plan.prob_n[plan.order]])
+        csize = route_large(plan.prob_n, self.large_threshold, self.large_cluster)[plan.order]
+        large = csize > 0
         out = []
-        for sfx in dict.fromkeys(shapes.tolist()):
-            sel = plan.order[shapes == sfx]
-            out.append((sfx, _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))
+        for c in sorted(set(csize[large].tolist()), reverse=True):    # one launch per cluster size
+            sel = plan.order[csize == c]
+            out.append((int(c), _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))
+        small_order = plan.order[~large]
+        if len(small_order):
+            if self.tuning is None:
+                shapes = np.array([""] * len(small_order))
+            else:
+                shapes = np.array([self.tuning.shape_for(int(n)) for n in plan.prob_n[small_order]])
+            for sfx in dict.fromkeys(shapes.tolist()):
+                sel = small_order[shapes == sfx]
+                out.append((sfx, _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))
+        if len(out) == 1 and out[0][0] == "" and out[0][2] == len(plan.order):
+            out = []     # the default launch over the batch's own order
         db._groups = (key, out)
         return out
 

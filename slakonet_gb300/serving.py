@@ -28,7 +28,7 @@ import torch
 from . import engine as E
 from .model import MultiElementSkfParameterOptimizer, properties_dict
 
-MAX_N = 2048   # single-CTA eigensolver bound (csrc/eigh.cu)
+MAX_N = E.LARGE_MAX_N   # cluster eigensolver bound (csrc/eigh_cluster.cu)
 
 
 def request_bytes(n_orb: int, nk: int, dos_points: int) -> int:

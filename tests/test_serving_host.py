@@ -49,7 +49,7 @@ def test_admission_budget_never_exceeded_and_all_requests_complete():
 
 def test_oversized_request_is_rejected_not_queued():
     sd = syn.default_shell_dict()
-    st = {"numbers": np.array([60] * 200), "positions": np.zeros((200, 3)), "cell": np.eye(3) * 50,
+    st = {"numbers": np.array([60] * 600), "positions": np.zeros((600, 3)), "cell": np.eye(3) * 50,   # 9600 orbitals
           "kpoints": np.zeros((1, 3))}
     server = SV.Server(FakeModel(), sd, device="cpu", mem_budget_bytes=1 << 30, n_workers=1,
                        executor=lambda s, stream: [{} for _ in s])
