@@ -369,6 +369,39 @@ def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40):
                         "each response: eigenvalues, DOS, gap, Fermi level"}
 
 
+def run_large_structure(dev):
+    """1000-atom Ga/As zincblende supercell (5x5x5 conventional cells, a = 5.65 A, 0.05 A jitter),
+    spd on both species (n = 9000), Gamma plus the 7 other points of the 2x2x2 Gamma-centred grid:
+    the whole path once, each k-point on a 16-CTA cluster eigensolver."""
+    import torch
+    from slakonet_gb300 import engine as E, synthetic as syn
+    st = syn.zincblende_supercell()
+    sd = {31: [0, 1, 2], 33: [0, 1, 2]}
+    tables = syn.make_tables([31, 33], sd, seed=SEED)
+    st["kpoints"] = syn.gamma_centred_kpoints((2, 2, 2))
+    st["weights"] = np.full(8, 1.0 / 8)
+    ts = E.TableSet.from_synthetic(tables, sd, dev)
+    plan = E.plan_batch([st], ts)
+    eng = E.Engine(ts)
+    eng.event_log = []
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    res = eng.run(plan, dos_range=DOS_RANGE, dos_points=DOS_POINTS, dos_window=DOS_WINDOW)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    phases = {}
+    for name, a, b in eng.event_log:
+        phases[name] = phases.get(name, 0.0) + a.elapsed_time(b) * 1e-3
+    n = int(plan.max_n)
+    flops = 32.0 / 3.0 * n ** 3 * len(plan.prob_n)
+    eig_s = phases.get("eigensolve", wall)
+    return {"atoms": len(st["numbers"]), "n": n, "k_points": len(plan.prob_n),
+            "eig_status_ok": int((res.eig_status == 0).sum()), "wall_s": wall,
+            "phase_s": {k: round(v, 4) for k, v in phases.items()},
+            "eigensolve_tflops": flops / eig_s * 1e-12, "gap_eV": float(res.stats[0, E.STAT["gap_ev"]]),
+            "note": "k-points on 16-CTA cluster eigensolvers (skn_eigh_gen_large), one cluster per k-point"}
+
+
 def run_cpu_baseline(sts, tables, sd, reps=1):
     _single_thread_workers()
     sample = cpu_sample(sts)
@@ -424,6 +457,8 @@ def main():
     ap.add_argument("--seed", type=int, default=SEED)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the training-step and serving measurements")
+    ap.add_argument("--large-structure", action="store_true",
+                    help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -444,6 +479,10 @@ def main():
             out["training_step"] = run_training_step(dev)
             log("serving")
             out["serving"] = run_serving(dev)
+        if world == 1 and args.large_structure:
+            import torch
+            log("large structure")
+            out["large_structure"] = run_large_structure(torch.device("cuda", 0))
         if world == 1 and not args.no_cpu_baseline:
             log("cpu baseline")
             out["cpu_baseline"] = run_cpu_baseline(sts, tables, sd)
