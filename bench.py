@@ -43,6 +43,11 @@ DOS_POINTS = 1000
 DOS_SIGMA = 0.1
 DOS_WINDOW = 9.0
 SAMPLE_STRIDE = 16         # CPU baseline: every 16th structure (stratified over sizes)
+# DRAM bytes (read + write) of one eigensolver launch on the default workload (256 structures, seed 0),
+# from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_eigh_gen`
+# on `bench.py --steps 1 --warmup 1 --no-cpu-baseline --no-extras` (one pass per launch): 0.950 TB read +
+# 0.509 TB written per launch
+EIG_TRAFFIC_BYTES = 1.459e12
 WORKLOAD = ("uneven batch: 256 random periodic structures, 2-64 atoms log-uniform, Z=1-65 default shells, "
             "Gamma-centred k-grids ~1000 k-atoms, FP64 generalized eigensolve per k, Fermi/gap, "
             "1000-pt DOS on [-20,10] eV")
@@ -290,7 +295,11 @@ def run_gpu(args, rank, world):
                    "autotune_batch_trials_ms": tuning.timings.get("batch_trials_ms")},
         "roofline": {"bound": "tensor", "kernel": "k_eigh_gen (skn_eigh_gen_batched, autotuned launch shapes)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": None,
+                     "traffic": (EIG_TRAFFIC_BYTES if (args.structures, args.seed) == (N_STRUCT, SEED)
+                                 else None),
+                     "traffic_note": "DRAM bytes per eigensolver launch (ncu); H(k)+S(k) are "
+                                     f"{2 * 16 * plan.hs_total / 1e9:.1f} GB, re-streamed from HBM every column "
+                                     "pass because the 760 problems in flight hold more than L2",
                      "peak_source": "measured in this run: FP64 FMA probe kernel (GB300 FP64 tensor MMA runs at "
                                     "the same rate, so this is the FP64 roofline)",
                      "algorithmic": "32/3 n^3 real flops per k (zpotrf 4/3 + zhegst 4 + zhetrd 16/3)",

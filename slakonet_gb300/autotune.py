@@ -10,6 +10,8 @@ the groups on forked streams so they share the GPU.
 """
 from __future__ import annotations
 
+import argparse
+import ctypes
 import hashlib
 import json
 import os
@@ -90,6 +92,44 @@ def time_shape(suffix: str, n: int, count: int, device, reps: int = 2) -> float:
         torch.cuda.synchronize(device)
         if r:
             best = min(best, a.elapsed_time(b) * 1e-3)
+    return best
+
+
+def time_cluster(n: int, count: int, cluster: int, device, reps: int = 1) -> float:
+    """Seconds for ``count`` random problems of n orbitals on the cluster eigensolver
+    (``cluster`` CTAs per problem); cluster 0 times the one-CTA-per-problem kernel."""
+    H0, S0 = _problems(n, count, device)
+    nv = torch.full((count,), n, dtype=torch.int32, device=device)
+    off = torch.arange(count, dtype=torch.int64, device=device) * n * n
+    eoff = torch.arange(count, dtype=torch.int64, device=device) * n
+    order = torch.arange(count, dtype=torch.int32, device=device)
+    eig = torch.empty(count * n, dtype=torch.float64, device=device)
+    st = torch.empty(count, dtype=torch.int32, device=device)
+    ctr = torch.zeros(2, dtype=torch.int32, device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    scratch, need = None, ctypes.c_int64(0)
+    if cluster:
+        call("skn_eigh_large_scratch_bytes", count, n, cluster, ctypes.addressof(need))
+        scratch = torch.empty(max(need.value // 8, 1), dtype=torch.float64, device=device)
+    best = float("inf")
+    for _ in range(reps):
+        H = torch.view_as_real(H0.clone()).reshape(-1)
+        S = torch.view_as_real(S0.clone()).reshape(-1)
+        torch.cuda.synchronize(device)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        if cluster:
+            call("skn_eigh_gen_large", count, ptr(nv), ptr(off), ptr(eoff), ptr(order), ptr(H), ptr(S), ptr(eig),
+                 ptr(st), ptr(ctr), ptr(scratch), need.value, n, cluster, stream)
+        else:
+            call("skn_eigh_gen_batched", count, ptr(nv), ptr(off), ptr(eoff), ptr(order), ptr(H), ptr(S), ptr(eig),
+                 ptr(st), ptr(ctr), n, stream)
+        b.record()
+        torch.cuda.synchronize(device)
+        best = min(best, a.elapsed_time(b) * 1e-3)
+    if int((st != 0).sum()):
+        raise _lib.SknError("random test problems failed to solve")
     return best
 
 
@@ -193,3 +233,24 @@ def tune_batch(engine, db, candidates: Optional[List[Tuning]] = None, reps: int 
     best.timings = dict(best.timings)
     best.timings["batch_trials_ms"] = timings
     return best
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="Time the eigensolver kernels on random Hermitian-definite problems.")
+    ap.add_argument("--n", type=int, nargs="+", default=[1024], help="orbitals per problem")
+    ap.add_argument("--count", type=int, default=1, help="problems per launch")
+    ap.add_argument("--clusters", type=int, nargs="+", default=[16],
+                    help="CTAs per problem on the cluster eigensolver; 0 = one-CTA-per-problem kernel")
+    ap.add_argument("--reps", type=int, default=1)
+    args = ap.parse_args(argv)
+    dev = torch.device("cuda", 0)
+    _lib.load()
+    out = {}
+    for n in args.n:
+        for c in args.clusters:
+            out[f"n{n}_c{c}"] = round(time_cluster(n, args.count, c, dev, args.reps), 6)
+    print(json.dumps({"count": args.count, "seconds": out}))
+
+
+if __name__ == "__main__":
+    main()

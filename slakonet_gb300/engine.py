@@ -348,10 +348,12 @@ def cluster_for(n: int) -> int:
     """CTAs (SMs) the cluster eigensolver gives one problem of n orbitals.
 
     Measured on GB300 (one problem alone, random Hermitian-definite pairs): at n = 1024
-    one SM takes 3.6 s, clusters of 2/4/8/16 CTAs 1.27/1.03/0.91/0.86 s; at n = 2048 one
-    SM takes 27 s and clusters 8.0/5.2/4.3/3.8 s.  Four CTAs keep most of the gain up to
-    2048 while 38 problems still run at once; larger problems get 8, then 16."""
-    return 4 if n <= 2048 else (8 if n <= 4096 else 16)
+    one SM takes 3.5 s, clusters of 4/8/16 CTAs 0.78/0.61/0.53 s; at n = 2048 clusters of
+    4/8/16 take 4.5/3.2/2.5 s; at n = 4096, 8/16 take 18.5/13.2 s.  Clusters that fit at
+    once: 36 of 4 CTAs, 15 of 8, 8 of 12, 7 of 16.  Four CTAs keep most of the gain up to
+    2048 orbitals; 8 up to 4096; above that 12, so that a structure's 8 k-points (a 2x2x2
+    grid) all run at once."""
+    return 4 if n <= 2048 else (8 if n <= 4096 else 12)
 
 
 def route_large(prob_n: np.ndarray, threshold: Optional[int] = 1024, cluster: Optional[int] = None) -> np.ndarray:

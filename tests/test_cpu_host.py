@@ -127,11 +127,11 @@ def test_engine_refuses_cpu():
 def test_large_problem_routing_depends_on_each_problem_alone():
     n = np.array([18, 300, 1024, 1025, 2048, 2049, 4096, 4097, 9000])
     sizes = E.route_large(n)
-    assert sizes.tolist() == [0, 0, 0, 4, 4, 8, 8, 16, 16]
+    assert sizes.tolist() == [0, 0, 0, 4, 4, 8, 8, 12, 12]
     # the same problem gets the same path whatever else is in the batch
     for other in (np.array([5000] * 7), np.array([20] * 1000)):
         both = E.route_large(np.concatenate([n, other]))
         assert both[:len(n)].tolist() == sizes.tolist()
     # no threshold: only problems above the one-CTA bound move; a fixed cluster size overrides
-    assert E.route_large(n, None).tolist() == [0, 0, 0, 0, 0, 8, 8, 16, 16]
+    assert E.route_large(n, None).tolist() == [0, 0, 0, 0, 0, 8, 8, 12, 12]
     assert E.route_large(n, 0, 2).tolist() == [2] * len(n)

@@ -75,7 +75,7 @@ def _solve(Hs, Ss, cluster=None):
     return [e[eoff[p]:eoff[p] + sizes[p]] for p in range(n_prob)], st.cpu().numpy()
 
 
-@pytest.mark.parametrize("cluster", [1, 2, 4, 8, 16])
+@pytest.mark.parametrize("cluster", [1, 2, 3, 4, 8, 12, 16])
 def test_cluster_sizes_agree_with_single_cta_and_lapack(cluster):
     sizes = [1, 2, 7, 33, 130, 257, 301]   # odd largest n: per-cluster scratch alignment
     Hs, Ss = _problems(sizes, seed=cluster)

@@ -1,4 +1,7 @@
-"""Continuous-batching server on the GPU: results alone equal results in the mix."""
+"""Continuous-batching server on the GPU: results alone equal results in the mix.
+
+The mix includes two structures of more than 1024 orbitals, whose k-points run
+on the cluster eigensolver, so both eigensolver paths are covered."""
 import numpy as np
 import pytest
 import torch
@@ -18,6 +21,12 @@ def test_results_identical_alone_and_in_the_mix():
         st["kpoints"] = syn.gamma_centred_kpoints(syn.gamma_centred_grid(st["cell"], len(st["numbers"]), 200))
         st["weights"] = np.full(len(st["kpoints"]), 1.0 / len(st["kpoints"]))
         sts.append(st)
+    for pos, n_atoms in ((7, 130), (23, 140)):      # 9 orbitals per atom (Z = 21..30): n > 1024
+        st = syn.random_structure(rng, n_atoms, zmax=30)
+        st["numbers"] = 21 + (np.asarray(st["numbers"]) % 10)
+        st["kpoints"] = syn.gamma_centred_kpoints((1, 1, 2))
+        st["weights"] = np.full(2, 0.5)
+        sts.insert(pos, st)
     zs = sorted({int(z) for st in sts for z in st["numbers"]})
     sd = syn.default_shell_dict()
     tables = syn.make_tables(zs, sd, seed=4)
