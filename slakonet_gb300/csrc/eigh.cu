@@ -5,8 +5,10 @@
 //   2. reduction to C = L^-1 H L^-H (LAPACK zhegs2 order: scale, axpy,
 //      her2, axpy, triangular solve per column),
 //   3. Householder tridiagonalisation of C (zhetd2: larfg, hemv, her2),
-//   4. eigenvalues of the real tridiagonal by Sturm-count bisection, one
-//      thread per eigenvalue, which returns them in ascending order.
+//   4. eigenvalues of the real tridiagonal from Sturm counts (FP32 bracket,
+//      then FP64 Newton on the characteristic polynomial for isolated
+//      eigenvalues, FP64 bisection for clusters), one thread per eigenvalue,
+//      which returns them in ascending order.
 // The reference runs torch.linalg.cholesky / solve / matmul / eigh per k
 // (slakonet/utils.py:741-783) in a serial Python loop (slakonet/main.py:174).
 //
@@ -19,7 +21,23 @@
 // per-column scalar steps.  Problems with n <= SMEM_N are staged in shared
 // memory; larger ones are factorised in place in global memory (L2-resident).
 #include "skn_common.cuh"
+#include "sturm.cuh"
 
+// Exported names carry SKN_EIG_SUFFIX so several launch shapes can live in one library.
+#ifndef SKN_EIG_SUFFIX
+#define SKN_EIG_SUFFIX
+#endif
+#define SKN_CAT2(a, b) a##b
+#define SKN_CAT(a, b) SKN_CAT2(a, b)
+#define SKN_EXPORT(name) SKN_CAT(name, SKN_EIG_SUFFIX)
+// Every compiled copy of this file keeps its kernels in its own namespace, so the
+// copies (launch shapes, and files that include this one) link side by side.
+#ifndef SKN_EIG_NS_TAG
+#define SKN_EIG_NS_TAG SKN_EIG_SUFFIX
+#endif
+#define SKN_EIG_NS SKN_CAT(skn_eig, SKN_EIG_NS_TAG)
+
+namespace SKN_EIG_NS {
 namespace {
 
 // Launch shape knobs (compile-time; tuned by the size sweep):
@@ -35,13 +53,6 @@ namespace {
 #ifndef SKN_EIG_SMEM_N
 #define SKN_EIG_SMEM_N 24
 #endif
-// Exported names carry SKN_EIG_SUFFIX so several launch shapes can live in one library.
-#ifndef SKN_EIG_SUFFIX
-#define SKN_EIG_SUFFIX
-#endif
-#define SKN_CAT2(a, b) a##b
-#define SKN_CAT(a, b) SKN_CAT2(a, b)
-#define SKN_EXPORT(name) SKN_CAT(name, SKN_EIG_SUFFIX)
 constexpr int NT = SKN_EIG_NT;    // threads per CTA
 constexpr int NW = NT / 32;
 constexpr int SMEM_N = SKN_EIG_SMEM_N;   // problems up to this size run from shared memory
@@ -132,65 +143,71 @@ __device__ bool cholesky_lower(double2* __restrict__ A, int lda, int n, Vecs& V)
 
 // y[i] = scale * sum_j Herm(A22)[i][j] x[j] for i < m, A22 at A (lower stored),
 // x in shared memory.  Rows on lanes with a uniform trip count over j, UNR
-// loads in flight per thread; with fewer rows than threads, warps split the
-// j range and partial sums are combined through `part`.
+// loads in flight per thread.  Full passes take NT rows; the remaining
+// m mod NT rows (all rows when m < NT) go to as many warps as they fill, and
+// when that leaves warps over, the warps split the j range and partial sums
+// are combined through `part`.  No thread computes a row twice, so a warp
+// issues FP64 work only for rows that exist.
+__device__ __forceinline__ double2 hemv_row(const double2* __restrict__ A, int lda, int i, int j0, int j1,
+                                            const double2* __restrict__ x) {
+  double2 acc0 = make_double2(0.0, 0.0), acc1 = make_double2(0.0, 0.0);
+  int j = j0;
+  for (; j + UNR <= j1; j += UNR) {
+    double2 a[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int jj = j + u;
+      const bool up = jj > i;
+      a[u] = up ? A[jj + (int64_t)i * lda] : A[i + (int64_t)jj * lda];
+      a[u].y = cond_flip(a[u].y, up);
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; u += 2) {
+      acc0 = cfma(a[u], x[j + u], acc0);
+      acc1 = cfma(a[u + 1], x[j + u + 1], acc1);
+    }
+  }
+  for (; j < j1; ++j) {
+    const bool up = j > i;
+    double2 a = up ? A[j + (int64_t)i * lda] : A[i + (int64_t)j * lda];
+    a.y = cond_flip(a.y, up);
+    acc0 = cfma(a, x[j], acc0);
+  }
+  return make_double2(acc0.x + acc1.x, acc0.y + acc1.y);
+}
+
 __device__ void hemv_lower(const double2* __restrict__ A, int lda, int m, const double2* __restrict__ x,
                            double2* __restrict__ y, double2 scale, double2* __restrict__ part) {
   const int tid = threadIdx.x;
-  const int row_warps = (m + 31) >> 5;
-  const int nsplit = row_warps >= NW ? 1 : NW / row_warps;
-  const int w = tid >> 5, lane = tid & 31;
-  const int rows_per_pass = (nsplit == 1) ? NT : row_warps * 32;
-  const int sp = (nsplit == 1) ? 0 : w / row_warps;
-  const int r_in = (nsplit == 1) ? tid : (w % row_warps) * 32 + lane;
-  const int chunk = (m + nsplit - 1) / nsplit;
-  const int j0 = sp * chunk, j1 = min(m, j0 + chunk);
-  for (int rbase = 0; rbase < m; rbase += rows_per_pass) {
-    const int i = min(rbase + r_in, m - 1);
-    double2 acc0 = make_double2(0.0, 0.0), acc1 = make_double2(0.0, 0.0);
-    if (sp < nsplit) {
-      int j = j0;
-      for (; j + UNR <= j1; j += UNR) {
-        double2 a[UNR];
-#pragma unroll
-        for (int u = 0; u < UNR; ++u) {
-          const int jj = j + u;
-          const bool up = jj > i;
-          a[u] = up ? A[jj + (int64_t)i * lda] : A[i + (int64_t)jj * lda];
-          a[u].y = cond_flip(a[u].y, up);
-        }
-#pragma unroll
-        for (int u = 0; u < UNR; u += 2) {
-          acc0 = cfma(a[u], x[j + u], acc0);
-          acc1 = cfma(a[u + 1], x[j + u + 1], acc1);
-        }
-      }
-      for (; j < j1; ++j) {
-        const bool up = j > i;
-        double2 a = up ? A[j + (int64_t)i * lda] : A[i + (int64_t)j * lda];
-        a.y = cond_flip(a.y, up);
-        acc0 = cfma(a, x[j], acc0);
-      }
-    }
-    acc0.x += acc1.x;
-    acc0.y += acc1.y;
+  const int full = (m / NT) * NT;
+  for (int rbase = 0; rbase < full; rbase += NT) y[rbase + tid] = cmul(scale, hemv_row(A, lda, rbase + tid, 0, m, x));
+  const int rem = m - full;
+  if (rem > 0) {
+    const int row_warps = (rem + 31) >> 5;            // <= NW
+    const int nsplit = NW / row_warps;
+    const int w = tid >> 5, lane = tid & 31;
+    const int sp = w / row_warps;
+    const int r_in = (w % row_warps) * 32 + lane;
+    const int i = full + min(r_in, rem - 1);
+    const int chunk = (m + nsplit - 1) / nsplit;
+    const int j0 = sp * chunk, j1 = min(m, j0 + chunk);
+    double2 acc = make_double2(0.0, 0.0);
+    if (sp < nsplit) acc = hemv_row(A, lda, i, j0, j1, x);
     if (nsplit == 1) {
-      if (rbase + r_in < m) y[rbase + r_in] = cmul(scale, acc0);
+      if (sp == 0 && r_in < rem) y[full + r_in] = cmul(scale, acc);
     } else {
-      part[tid] = acc0;
-    }
-  }
-  if (nsplit > 1) {
-    __syncthreads();
-    for (int r = tid; r < m; r += NT) {
-      double2 s = make_double2(0.0, 0.0);
-      const int rbw = r >> 5, ln = r & 31;
-      for (int q = 0; q < nsplit; ++q) {
-        const double2 v = part[(q * row_warps + rbw) * 32 + ln];
-        s.x += v.x;
-        s.y += v.y;
+      part[tid] = acc;
+      __syncthreads();
+      for (int r = tid; r < rem; r += NT) {
+        double2 s = make_double2(0.0, 0.0);
+        const int rbw = r >> 5, ln = r & 31;
+        for (int q = 0; q < nsplit; ++q) {
+          const double2 v = part[(q * row_warps + rbw) * 32 + ln];
+          s.x += v.x;
+          s.y += v.y;
+        }
+        y[full + r] = cmul(scale, s);
       }
-      y[r] = cmul(scale, s);
     }
   }
   __syncthreads();
@@ -432,57 +449,10 @@ __device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V, do
   }
 }
 
-// ------------------------------------------------------- Sturm bisection
-// Number of eigenvalues of the tridiagonal (d, e^2) below x.
-//
-// FP64 count: the determinant recurrence p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}
-// (three FP64 operations per step, no division); the count is the number of
-// sign changes of p_0..p_n, i.e. of negative pivots q_i = p_i / p_{i-1} of
-// the LDL^T factorisation of T - x I.  Signs are read from the bit pattern
-// and the pair (p, p_prev) is rescaled by exact powers of two when its
-// exponent drifts, so nothing overflows.  An exact zero p_i takes the sign
-// opposite to p_{i-1} (the tiny negative pivot LAPACK substitutes).
-__device__ __forceinline__ int sign_bit(double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 63); }
-
-__device__ int sturm_count64(const double* d, const double* e2, int n, double x) {
-  double pm = 1.0, p = d[0] - x;
-  if (is_zero_bits(p)) p = -0x1p-200;
-  int c = sign_bit(p);
-  int sp = c;
-  for (int i = 1; i < n; ++i) {
-    double pn = fma(-e2[i - 1], pm, (d[i] - x) * p);
-    if (is_zero_bits(pn)) pn = flip_sign(p) * 0x1p-200;
-    const int sn = sign_bit(pn);
-    c += sn ^ sp;
-    sp = sn;
-    pm = p;
-    p = pn;
-    const int ex = (int)((__double_as_longlong(p) >> 52) & 0x7ff);
-    if (ex > 1023 + 480 || ex < 1023 - 480) {
-      const double f = __longlong_as_double((long long)(2046 - ex) << 52);  // 2^(1023 - ex)
-      p *= f;
-      pm *= f;
-    }
-  }
-  return c;
-}
-
-// FP32 count on the rounded tridiagonal (LDL^T pivots, FP32 division is cheap).
-__device__ int sturm_count32(const float* d, const float* e2, int n, float x, float pivmin) {
-  float q = d[0] - x;
-  int c = q < 0.0f;
-  for (int i = 1; i < n; ++i) {
-    if (fabsf(q) < pivmin) q = -pivmin;
-    q = (d[i] - x) - __fdiv_rn(e2[i - 1], q);
-    c += q < 0.0f;
-  }
-  return c;
-}
-
-// Eigenvalue j of the tridiagonal: FP32 bisection brackets it to ~1e-6 of the
-// spectrum's scale, two FP64 counts confirm the widened bracket (else the
-// full Gershgorin interval is used), and FP64 bisection finishes it to
-// 1e-14 of the scale.
+// ------------------------------------------------------- tridiagonal eigenvalues
+// One thread per eigenvalue (csrc/sturm.cuh: FP32 bracket, FP64 Newton for
+// isolated eigenvalues, FP64 bisection for clusters).  The Gershgorin bounds
+// are reduced over the CTA first.
 __device__ void tridiag_eigenvalues(int n, Vecs& V, double* out) {
   const int tid = threadIdx.x;
   double lo = 1e300, hi = -1e300, emax = 0.0;
@@ -515,35 +485,9 @@ __device__ void tridiag_eigenvalues(int n, Vecs& V, double* out) {
     hi = fmax(hi, V.red[NW + w]);
     emax = fmax(emax, V.red[2 * NW + w]);
   }
-  const double bnorm = fmax(fmax(fabs(lo), fabs(hi)), 1e-300);
-  lo -= 2.2e-16 * bnorm * 4.0 * n + 1e-300;
-  hi += 2.2e-16 * bnorm * 4.0 * n + 1e-300;
-  const double atol = 1e-14 * bnorm;
-  const float pivmin32 = 1.1754944e-38f * fmaxf(1.0f, (float)emax);
-  const double margin = 32.0 * 5.9604645e-8 * bnorm;   // covers FP32 rounding of T and of the count
+  const skn_sturm::Bounds B = skn_sturm::make_bounds(lo, hi, emax, n);
   __syncthreads();
-  for (int j = tid; j < n; j += NT) {
-    // FP32 bracket
-    float a32 = (float)lo, b32 = (float)hi;
-    for (int it = 0; it < 40; ++it) {
-      const float mid = 0.5f * (a32 + b32);
-      if (!(mid > a32 && mid < b32)) break;
-      if (sturm_count32(V.d32, V.e232, n, mid, pivmin32) > j) b32 = mid; else a32 = mid;
-    }
-    double a = (double)a32 - margin, b = (double)b32 + margin;
-    if (a < lo) a = lo;
-    if (b > hi) b = hi;
-    if (!(sturm_count64(V.d, V.e2, n, a) <= j && sturm_count64(V.d, V.e2, n, b) > j)) {
-      a = lo;
-      b = hi;
-    }
-    for (int it = 0; it < 200 && (b - a) > atol; ++it) {
-      const double mid = 0.5 * (a + b);
-      if (mid <= a || mid >= b) break;
-      if (sturm_count64(V.d, V.e2, n, mid) > j) b = mid; else a = mid;
-    }
-    out[j] = 0.5 * (a + b);
-  }
+  for (int j = tid; j < n; j += NT) out[j] = skn_sturm::eigenvalue(V.d, V.e2, V.d32, V.e232, n, j, B);
 }
 
 // Unit diagonal for rows/columns that are entirely zero (eighb's aux option,
@@ -868,6 +812,8 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
   }
 }
 }  // namespace
+}  // namespace SKN_EIG_NS
+using namespace SKN_EIG_NS;
 
 // Dynamic shared-memory limits are per-function attributes.  They are set to
 // the largest size any call can request (max_n = MAX_N), so concurrent calls

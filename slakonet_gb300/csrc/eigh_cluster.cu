@@ -3,7 +3,7 @@
 //
 // Same steps as k_eigh_gen in eigh.cu (unit diagonal for zero rows, Cholesky
 // S = L L^H, reduction to L^-1 H L^-H in zhegs2 column order, zhetd2
-// Householder tridiagonalisation, Sturm bisection), but the C CTAs of a
+// Householder tridiagonalisation, Sturm-count eigenvalues), but the C CTAs of a
 // cluster, one per SM, share one problem held in global memory: every
 // O(m^2)-per-column loop is split over all C*CNT threads of the cluster,
 // phases are separated by cluster barriers, and reductions go through
@@ -19,6 +19,7 @@
 // 64 rows per barrier: each CTA stages the 64x64 diagonal block of L in shared
 // memory and solves it itself).
 #include "skn_common.cuh"
+#include "sturm.cuh"
 #include <cooperative_groups.h>
 
 namespace cg = cooperative_groups;
@@ -132,43 +133,6 @@ __device__ void tri_update(double2* T, int lda, int m, const double2* x, const d
       }
     }
   }
-}
-
-__device__ __forceinline__ int sign_bit(double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 63); }
-
-// Sturm counts, as in eigh.cu: division-free FP64 determinant recurrence with
-// power-of-two rescaling, and FP32 LDL^T pivots for the bracket.
-__device__ int sturm64(const double* d, const double* e2, int n, double x) {
-  double pm = 1.0, p = d[0] - x;
-  if (is_zero_bits(p)) p = -0x1p-200;
-  int c = sign_bit(p), sp = c;
-  for (int i = 1; i < n; ++i) {
-    double pn = fma(-e2[i - 1], pm, (d[i] - x) * p);
-    if (is_zero_bits(pn)) pn = flip_sign(p) * 0x1p-200;
-    const int sn = sign_bit(pn);
-    c += sn ^ sp;
-    sp = sn;
-    pm = p;
-    p = pn;
-    const int ex = (int)((__double_as_longlong(p) >> 52) & 0x7ff);
-    if (ex > 1023 + 480 || ex < 1023 - 480) {
-      const double f = __longlong_as_double((long long)(2046 - ex) << 52);
-      p *= f;
-      pm *= f;
-    }
-  }
-  return c;
-}
-
-__device__ int sturm32(const float* d, const float* e2, int n, float x, float pivmin) {
-  float q = d[0] - x;
-  int c = q < 0.0f;
-  for (int i = 1; i < n; ++i) {
-    if (fabsf(q) < pivmin) q = -pivmin;
-    q = (d[i] - x) - __fdiv_rn(e2[i - 1], q);
-    c += q < 0.0f;
-  }
-  return c;
 }
 
 __device__ __forceinline__ double2 csub_mul(double2 v, double2 x, double2 l) {   // v - x * l
@@ -514,7 +478,7 @@ __global__ void __launch_bounds__(CNT, 1) k_eigh_cluster(int n_prob, const int32
     if (lead) V.d[n - 1] = ldc(A + (n - 1) + (int64_t)(n - 1) * lda).x;
     cl.sync();
 
-    // ---------------------------------------------------------------- bisection
+    // ------------------------------------------------------- tridiagonal eigenvalues
     // Every CTA copies the tridiagonal into its shared memory and derives the
     // same Gershgorin bounds.
     double lo = 1e300, hi = -1e300, emax = 0.0;
@@ -553,33 +517,8 @@ __global__ void __launch_bounds__(CNT, 1) k_eigh_cluster(int n_prob, const int32
       hi = fmax(hi, red_warp[CNW + w]);
       emax = fmax(emax, red_warp[2 * CNW + w]);
     }
-    const double bnorm = fmax(fmax(fabs(lo), fabs(hi)), 1e-300);
-    lo -= 2.2e-16 * bnorm * 4.0 * n + 1e-300;
-    hi += 2.2e-16 * bnorm * 4.0 * n + 1e-300;
-    const double atol = 1e-14 * bnorm;
-    const float pivmin32 = 1.1754944e-38f * fmaxf(1.0f, (float)emax);
-    const double margin = 32.0 * 5.9604645e-8 * bnorm;
-    for (int j = gt; j < n; j += GT) {
-      float a32 = (float)lo, b32 = (float)hi;
-      for (int it = 0; it < 40; ++it) {
-        const float mid = 0.5f * (a32 + b32);
-        if (!(mid > a32 && mid < b32)) break;
-        if (sturm32(sd32, se232, n, mid, pivmin32) > j) b32 = mid; else a32 = mid;
-      }
-      double a = (double)a32 - margin, b = (double)b32 + margin;
-      if (a < lo) a = lo;
-      if (b > hi) b = hi;
-      if (!(sturm64(sd, se2, n, a) <= j && sturm64(sd, se2, n, b) > j)) {
-        a = lo;
-        b = hi;
-      }
-      for (int it = 0; it < 200 && (b - a) > atol; ++it) {
-        const double mid = 0.5 * (a + b);
-        if (mid <= a || mid >= b) break;
-        if (sturm64(sd, se2, n, mid) > j) b = mid; else a = mid;
-      }
-      eig[eig_off[p] + j] = 0.5 * (a + b);
-    }
+    const skn_sturm::Bounds Bd = skn_sturm::make_bounds(lo, hi, emax, n);
+    for (int j = gt; j < n; j += GT) eig[eig_off[p] + j] = skn_sturm::eigenvalue(sd, se2, sd32, se232, n, j, Bd);
     if (lead) status[p] = SKN_OK;
     cl.sync();   // the next problem reuses the cluster's vectors and shared memory
   }

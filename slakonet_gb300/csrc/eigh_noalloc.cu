@@ -9,6 +9,7 @@
 // file is loaded, once per device, and its device address is looked up once
 // per device on the first call.
 #define SKN_EIG_KERNELS_ONLY
+#define SKN_EIG_NS_TAG _noalloc
 #include "eigh.cu"
 
 #include <mutex>
