@@ -151,6 +151,18 @@ int skn_eigh_gen_batched(int n_prob, const int32_t* n, const int64_t* hs_off, co
                          int32_t* work_counter, int max_n, cudaStream_t stream);
 
 /*
+ * skn_eigh_gen_batched for problems whose H and S are real symmetric (every
+ * imaginary part zero, e.g. the Bloch sums at k-points with 2k integer):
+ * only the real parts are read and written, in real arithmetic (a quarter of
+ * the FP64 work).  The steps are those of skn_eigh_gen_batched minus terms
+ * that are exactly zero for real input, so the eigenvalues are the same.
+ * Imaginary parts are ignored, not checked: route only real problems here.
+ */
+int skn_eigh_gen_batched_real(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                              const int32_t* order, double* H, double* S, double* eig, int32_t* status,
+                              int32_t* work_counter, int max_n, cudaStream_t stream);
+
+/*
  * Eigenvalues and eigenvectors of the same batched problems.  Replaces the
  * eigenvector output of eighb (slakonet/utils.py:741-783) that
  * SimpleDftb.__call__ keeps with with_eigenvectors (slakonet/main.py:137-196).
@@ -239,6 +251,12 @@ int skn_eigh_gen_vectors_t256(int n_prob, const int32_t* n, const int64_t* hs_of
                               const int32_t* order, double* H, double* S, double* eig, double* vec,
                               int32_t* status, double* tri, double* scratch, int64_t scratch_bytes,
                               int32_t* work_counter, int max_n, cudaStream_t stream);
+int skn_eigh_gen_batched_real_t64(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                                  const int32_t* order, double* H, double* S, double* eig, int32_t* status,
+                                  int32_t* work_counter, int max_n, cudaStream_t stream);
+int skn_eigh_gen_batched_real_t256(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                                   const int32_t* order, double* H, double* S, double* eig, int32_t* status,
+                                   int32_t* work_counter, int max_n, cudaStream_t stream);
 int skn_eigh_vectors_scratch_bytes_t64(int n_prob, int max_n, int64_t* bytes);
 int skn_eigh_vectors_scratch_bytes_t256(int n_prob, int max_n, int64_t* bytes);
 

@@ -39,6 +39,7 @@ SIGNATURES = {
     "skn_sk_blocks": [I64, P, P, P, P, P, P, I32, P, P, P, P, P, P, P, P, P, P, P, P, P],
     "skn_bloch": [I32, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, I32, P, P, P],
     "skn_eigh_gen_batched": [I32, P, P, P, P, P, P, P, P, P, I32, P],
+    "skn_eigh_gen_batched_real": [I32, P, P, P, P, P, P, P, P, P, I32, P],
     "skn_fermi_gap": [I32, P, P, P, P, P, P, P, F64, F64, I32, P, P, P, P],
     "skn_dos": [I32, P, P, P, P, P, P, P, F64, F64, I32, F64, F64, P, P, P, P],
     "skn_fp64_probe": [P, I32, I32, P],
@@ -54,6 +55,7 @@ SIGNATURES = {
 }
 for _sfx in ("_t64", "_t256"):
     SIGNATURES["skn_eigh_gen_batched" + _sfx] = SIGNATURES["skn_eigh_gen_batched"]
+    SIGNATURES["skn_eigh_gen_batched_real" + _sfx] = SIGNATURES["skn_eigh_gen_batched"]
     SIGNATURES["skn_eigh_gen_vectors" + _sfx] = SIGNATURES["skn_eigh_gen_vectors"]
     SIGNATURES["skn_eigh_vectors_scratch_bytes" + _sfx] = SIGNATURES["skn_eigh_vectors_scratch_bytes"]
 

@@ -85,6 +85,46 @@ __device__ __forceinline__ double2 cfms_conj_l(double2 a, double2 b, double2 c) 
   return c;
 }
 
+// Arithmetic on complex entries, or on their real parts alone when the problem
+// is real (R = true: every imaginary part of H and S is exactly zero, as at
+// k-points with 2k integer, where the Bloch phases are exactly +-1).  With R
+// the imaginary parts are never loaded, computed or stored; each real part
+// comes out of the same fused operations as in the complex code, minus terms
+// that are exactly zero, so both paths give the same numbers on a real problem
+// while the real one issues a quarter of the FP64 instructions.
+template <bool R> SKN_DEVINL double2 z_ld(const double2* p) {
+  if constexpr (R) return make_double2(p->x, 0.0); else return *p;
+}
+template <bool R> SKN_DEVINL void z_st(double2* p, double2 v) {
+  if constexpr (R) p->x = v.x; else *p = v;
+}
+template <bool R> SKN_DEVINL double2 z_fma(double2 a, double2 b, double2 c) {   // c + a b
+  if constexpr (R) { c.x = fma(a.x, b.x, c.x); return c; } else return cfma(a, b, c);
+}
+template <bool R> SKN_DEVINL double2 z_fms_conj(double2 a, double2 b, double2 c) {   // c - a conj(b)
+  if constexpr (R) { c.x = fma(-a.x, b.x, c.x); return c; } else return cfms_conj(a, b, c);
+}
+template <bool R> SKN_DEVINL double2 z_mul(double2 a, double2 b) {
+  if constexpr (R) return make_double2(a.x * b.x, 0.0); else return cmul(a, b);
+}
+template <bool R> SKN_DEVINL double2 z_scale(double2 a, double s) {
+  if constexpr (R) return make_double2(a.x * s, 0.0); else return cscale(a, s);
+}
+template <bool R> SKN_DEVINL double2 z_axpy(double a, double2 x, double2 y) {   // y + a x, a real
+  y.x = fma(a, x.x, y.x);
+  if constexpr (!R) y.y = fma(a, x.y, y.y);
+  return y;
+}
+template <bool R> SKN_DEVINL double2 z_sub_mul(double2 v, double2 x, double2 l) {   // v - x l
+  v.x = fma(-x.x, l.x, v.x);
+  if constexpr (!R) {
+    v.x = fma(x.y, l.y, v.x);
+    v.y = fma(-x.x, l.y, v.y);
+    v.y = fma(-x.y, l.x, v.y);
+  }
+  return v;
+}
+
 // ---------------------------------------------------------------- Cholesky
 // Loops over the trailing triangle issue UNR independent loads per thread
 // before their FMAs: with FP64 this slow, the kernel is bound by how many
@@ -92,6 +132,7 @@ __device__ __forceinline__ double2 cfms_conj_l(double2 a, double2 b, double2 c) 
 constexpr int UNR = SKN_EIG_UNR;
 static_assert(UNR >= 2 && UNR % 2 == 0, "unrolled loops pair their accumulators");
 
+template <bool R>
 __device__ bool cholesky_lower(double2* __restrict__ A, int lda, int n, Vecs& V) {
   const int tid = threadIdx.x;
   for (int k = 0; k < n; ++k) {
@@ -111,8 +152,8 @@ __device__ bool cholesky_lower(double2* __restrict__ A, int lda, int n, Vecs& V)
     const int m = n - k - 1;
     double2* col = A + (k + 1) + (int64_t)k * lda;
     for (int i = tid; i < m; i += NT) {
-      const double2 v = cscale(col[i], rd);
-      col[i] = v;
+      const double2 v = z_scale<R>(z_ld<R>(col + i), rd);
+      z_st<R>(col + i, v);
       V.v[i] = v;
     }
     __syncthreads();
@@ -128,12 +169,12 @@ __device__ bool cholesky_lower(double2* __restrict__ A, int lda, int n, Vecs& V)
         if (e < tri) {
           tri_index(e, m, ii[u], jj[u]);
           off[u] = ii[u] + jj[u] * lda;
-          a[u] = T[off[u]];
+          a[u] = z_ld<R>(T + off[u]);
         }
       }
 #pragma unroll
       for (int u = 0; u < UNR; ++u) {
-        if (e0 + u * NT < tri) T[off[u]] = cfms_conj(V.v[ii[u]], V.v[jj[u]], a[u]);
+        if (e0 + u * NT < tri) z_st<R>(T + off[u], z_fms_conj<R>(V.v[ii[u]], V.v[jj[u]], a[u]));
       }
     }
     __syncthreads();
@@ -148,6 +189,7 @@ __device__ bool cholesky_lower(double2* __restrict__ A, int lda, int n, Vecs& V)
 // when that leaves warps over, the warps split the j range and partial sums
 // are combined through `part`.  No thread computes a row twice, so a warp
 // issues FP64 work only for rows that exist.
+template <bool R>
 __device__ __forceinline__ double2 hemv_row(const double2* __restrict__ A, int lda, int i, int j0, int j1,
                                             const double2* __restrict__ x) {
   double2 acc0 = make_double2(0.0, 0.0), acc1 = make_double2(0.0, 0.0);
@@ -158,29 +200,30 @@ __device__ __forceinline__ double2 hemv_row(const double2* __restrict__ A, int l
     for (int u = 0; u < UNR; ++u) {
       const int jj = j + u;
       const bool up = jj > i;
-      a[u] = up ? A[jj + (int64_t)i * lda] : A[i + (int64_t)jj * lda];
-      a[u].y = cond_flip(a[u].y, up);
+      a[u] = z_ld<R>(up ? A + jj + (int64_t)i * lda : A + i + (int64_t)jj * lda);
+      if constexpr (!R) a[u].y = cond_flip(a[u].y, up);
     }
 #pragma unroll
     for (int u = 0; u < UNR; u += 2) {
-      acc0 = cfma(a[u], x[j + u], acc0);
-      acc1 = cfma(a[u + 1], x[j + u + 1], acc1);
+      acc0 = z_fma<R>(a[u], x[j + u], acc0);
+      acc1 = z_fma<R>(a[u + 1], x[j + u + 1], acc1);
     }
   }
   for (; j < j1; ++j) {
     const bool up = j > i;
-    double2 a = up ? A[j + (int64_t)i * lda] : A[i + (int64_t)j * lda];
-    a.y = cond_flip(a.y, up);
-    acc0 = cfma(a, x[j], acc0);
+    double2 a = z_ld<R>(up ? A + j + (int64_t)i * lda : A + i + (int64_t)j * lda);
+    if constexpr (!R) a.y = cond_flip(a.y, up);
+    acc0 = z_fma<R>(a, x[j], acc0);
   }
   return make_double2(acc0.x + acc1.x, acc0.y + acc1.y);
 }
 
+template <bool R>
 __device__ void hemv_lower(const double2* __restrict__ A, int lda, int m, const double2* __restrict__ x,
                            double2* __restrict__ y, double2 scale, double2* __restrict__ part) {
   const int tid = threadIdx.x;
   const int full = (m / NT) * NT;
-  for (int rbase = 0; rbase < full; rbase += NT) y[rbase + tid] = cmul(scale, hemv_row(A, lda, rbase + tid, 0, m, x));
+  for (int rbase = 0; rbase < full; rbase += NT) y[rbase + tid] = z_mul<R>(scale, hemv_row<R>(A, lda, rbase + tid, 0, m, x));
   const int rem = m - full;
   if (rem > 0) {
     const int row_warps = (rem + 31) >> 5;            // <= NW
@@ -192,9 +235,9 @@ __device__ void hemv_lower(const double2* __restrict__ A, int lda, int m, const 
     const int chunk = (m + nsplit - 1) / nsplit;
     const int j0 = sp * chunk, j1 = min(m, j0 + chunk);
     double2 acc = make_double2(0.0, 0.0);
-    if (sp < nsplit) acc = hemv_row(A, lda, i, j0, j1, x);
+    if (sp < nsplit) acc = hemv_row<R>(A, lda, i, j0, j1, x);
     if (nsplit == 1) {
-      if (sp == 0 && r_in < rem) y[full + r_in] = cmul(scale, acc);
+      if (sp == 0 && r_in < rem) y[full + r_in] = z_mul<R>(scale, acc);
     } else {
       part[tid] = acc;
       __syncthreads();
@@ -206,7 +249,7 @@ __device__ void hemv_lower(const double2* __restrict__ A, int lda, int m, const 
           s.x += v.x;
           s.y += v.y;
         }
-        y[full + r] = cmul(scale, s);
+        y[full + r] = z_mul<R>(scale, s);
       }
     }
   }
@@ -214,6 +257,7 @@ __device__ void hemv_lower(const double2* __restrict__ A, int lda, int m, const 
 }
 
 // A22 -= x y^H + y x^H on the packed lower triangle (A22 at T), x and y in shared memory.
+template <bool R>
 __device__ void her2_lower(double2* __restrict__ T, int lda, int m, const double2* __restrict__ x,
                            const double2* __restrict__ y) {
   const int tri = m * (m + 1) / 2;
@@ -226,14 +270,14 @@ __device__ void her2_lower(double2* __restrict__ T, int lda, int m, const double
       if (e < tri) {
         tri_index(e, m, ii[u], jj[u]);
         off[u] = ii[u] + jj[u] * lda;
-        a[u] = T[off[u]];
+        a[u] = z_ld<R>(T + off[u]);
       }
     }
 #pragma unroll
     for (int u = 0; u < UNR; ++u) {
       if (e0 + u * NT < tri) {
-        double2 v = cfms_conj(x[ii[u]], y[jj[u]], a[u]);
-        T[off[u]] = cfms_conj(y[ii[u]], x[jj[u]], v);
+        double2 v = z_fms_conj<R>(x[ii[u]], y[jj[u]], a[u]);
+        z_st<R>(T + off[u], z_fms_conj<R>(y[ii[u]], x[jj[u]], v));
       }
     }
   }
@@ -243,6 +287,7 @@ __device__ void her2_lower(double2* __restrict__ T, int lda, int m, const double
 // A (lower) <- L^-1 A L^-H with B = L from cholesky_lower (rdiag holds 1/L_kk),
 // column by column in LAPACK zhegs2 order.  The working column and the L
 // column live in shared memory for the rank-2 update and the solve.
+template <bool R>
 __device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __restrict__ B, int ldb, int n,
                             Vecs& V, double2* tile) {
   const int tid = threadIdx.x;
@@ -263,21 +308,15 @@ __device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __r
     double2* a = V.v;
     double2* b = V.w;
     for (int i = tid; i < m; i += NT) {
-      const double2 bi = bcol[i];
-      double2 v = cscale(acol[i], rd);
-      v.x = fma(ct, bi.x, v.x);
-      v.y = fma(ct, bi.y, v.y);
-      a[i] = v;
+      const double2 bi = z_ld<R>(bcol + i);
+      a[i] = z_axpy<R>(ct, bi, z_scale<R>(z_ld<R>(acol + i), rd));
       b[i] = bi;
     }
     __syncthreads();
-    her2_lower(A + (k + 1) + (int64_t)(k + 1) * lda, lda, m, a, b);
+    her2_lower<R>(A + (k + 1) + (int64_t)(k + 1) * lda, lda, m, a, b);
     __syncthreads();   // the update above reads a[]; the axpy below rewrites it
     for (int i = tid; i < m; i += NT) {
-      double2 v = a[i];
-      v.x = fma(ct, b[i].x, v.x);
-      v.y = fma(ct, b[i].y, v.y);
-      a[i] = v;
+      a[i] = z_axpy<R>(ct, b[i], a[i]);
     }
     __syncthreads();
     // forward substitution a <- L22^-1 a in chunks of 32 rows: warp 0 solves the
@@ -291,7 +330,7 @@ __device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __r
       if (tile != nullptr) {
         for (int e = tid; e < cm * 32; e += NT) {
           const int r = e & 31, c = e >> 5;
-          if (r < cm) tile[r + c * 33] = Ld[r + (int64_t)c * ldb];
+          if (r < cm) tile[r + c * 33] = z_ld<R>(Ld + r + (int64_t)c * ldb);
         }
         __syncthreads();
         Ld = tile;
@@ -301,16 +340,12 @@ __device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __r
         const int lane = tid;
         double2 xv = (lane < cm) ? a[c0 + lane] : make_double2(0.0, 0.0);
         for (int i = 0; i < cm; ++i) {
-          if (lane == i) xv = cscale(xv, V.rdiag[k + 1 + c0 + i]);
+          if (lane == i) xv = z_scale<R>(xv, V.rdiag[k + 1 + c0 + i]);
           double2 xi;
           xi.x = __shfl_sync(0xffffffffu, xv.x, i);
-          xi.y = __shfl_sync(0xffffffffu, xv.y, i);
+          xi.y = R ? 0.0 : __shfl_sync(0xffffffffu, xv.y, i);
           if (lane > i && lane < cm) {
-            const double2 l = Ld[lane + (int64_t)i * ldt];
-            xv.x = fma(-xi.x, l.x, xv.x);
-            xv.x = fma(xi.y, l.y, xv.x);
-            xv.y = fma(-xi.x, l.y, xv.y);
-            xv.y = fma(-xi.y, l.x, xv.y);
+            xv = z_sub_mul<R>(xv, xi, z_ld<R>(Ld + lane + (int64_t)i * ldt));
           }
         }
         if (lane < cm) a[c0 + lane] = xv;
@@ -325,32 +360,21 @@ __device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __r
         for (; i + UNR <= cm; i += UNR) {
           double2 l[UNR];
 #pragma unroll
-          for (int u = 0; u < UNR; ++u) l[u] = Lr[(int64_t)(i + u) * ldb];
+          for (int u = 0; u < UNR; ++u) l[u] = z_ld<R>(Lr + (int64_t)(i + u) * ldb);
 #pragma unroll
           for (int u = 0; u < UNR; u += 2) {
-            const double2 x0 = a[c0 + i + u], x1 = a[c0 + i + u + 1];
-            v0.x = fma(-x0.x, l[u].x, v0.x);
-            v0.x = fma(x0.y, l[u].y, v0.x);
-            v0.y = fma(-x0.x, l[u].y, v0.y);
-            v0.y = fma(-x0.y, l[u].x, v0.y);
-            v1.x = fma(-x1.x, l[u + 1].x, v1.x);
-            v1.x = fma(x1.y, l[u + 1].y, v1.x);
-            v1.y = fma(-x1.x, l[u + 1].y, v1.y);
-            v1.y = fma(-x1.y, l[u + 1].x, v1.y);
+            v0 = z_sub_mul<R>(v0, a[c0 + i + u], l[u]);
+            v1 = z_sub_mul<R>(v1, a[c0 + i + u + 1], l[u + 1]);
           }
         }
         for (; i < cm; ++i) {
-          const double2 x0 = a[c0 + i], l0 = Lr[(int64_t)i * ldb];
-          v0.x = fma(-x0.x, l0.x, v0.x);
-          v0.x = fma(x0.y, l0.y, v0.x);
-          v0.y = fma(-x0.x, l0.y, v0.y);
-          v0.y = fma(-x0.y, l0.x, v0.y);
+          v0 = z_sub_mul<R>(v0, a[c0 + i], z_ld<R>(Lr + (int64_t)i * ldb));
         }
         a[row] = make_double2(v0.x + v1.x, v0.y + v1.y);
       }
       __syncthreads();
     }
-    for (int i = tid; i < m; i += NT) acol[i] = a[i];
+    for (int i = tid; i < m; i += NT) z_st<R>(acol + i, a[i]);
     __syncthreads();
   }
 }
@@ -358,6 +382,7 @@ __device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __r
 // ------------------------------------------------------ tridiagonalisation
 // LAPACK zhetd2 (lower): reflector from column k, w = tau A22 v,
 // w -= (tau/2)(w^H v) v, A22 -= v w^H + w v^H.  d and e^2 go to shared memory.
+template <bool R>
 __device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V, double* tri) {
   const int tid = threadIdx.x;
   for (int k = 0; k < n - 1; ++k) {
@@ -365,13 +390,13 @@ __device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V, do
     double2* x = A + (k + 1) + (int64_t)k * lda;
     double s = 0.0;
     for (int i = 1 + tid; i < m; i += NT) {
-      const double2 xi = x[i];
+      const double2 xi = z_ld<R>(x + i);
       V.v[i] = xi;
-      s = fma(xi.x, xi.x, fma(xi.y, xi.y, s));
+      s = R ? fma(xi.x, xi.x, s) : fma(xi.x, xi.x, fma(xi.y, xi.y, s));
     }
     const double xnorm2 = block_sum(s, V.red);
     if (tid == 0) {
-      const double2 alpha = x[0];
+      const double2 alpha = z_ld<R>(x);
       double beta, taur, taui;
       double2 scl = make_double2(0.0, 0.0);
       int trivial = 0;
@@ -411,25 +436,29 @@ __device__ void hetd2_lower(double2* __restrict__ A, int lda, int n, Vecs& V, do
     if (!trivial) {
       const double2 scl = make_double2(V.sc[3], V.sc[4]);
       for (int i = 1 + tid; i < m; i += NT) {
-        const double2 v = cmul(V.v[i], scl);
+        const double2 v = z_mul<R>(V.v[i], scl);
         V.v[i] = v;
-        x[i] = v;
+        z_st<R>(x + i, v);
       }
       __syncthreads();
       double2* T = A + (k + 1) + (int64_t)(k + 1) * lda;
-      hemv_lower(T, lda, m, V.v, V.w, tau, reinterpret_cast<double2*>(V.red + 4 * NW));
+      hemv_lower<R>(T, lda, m, V.v, V.w, tau, reinterpret_cast<double2*>(V.red + 4 * NW));
       double pr = 0.0, pi = 0.0;
       for (int i = tid; i < m; i += NT) {
         const double2 wi = V.w[i], vi = V.v[i];
-        pr = fma(wi.x, vi.x, fma(wi.y, vi.y, pr));
-        pi = fma(wi.x, vi.y, fma(-wi.y, vi.x, pi));
+        if constexpr (R) {
+          pr = fma(wi.x, vi.x, pr);
+        } else {
+          pr = fma(wi.x, vi.x, fma(wi.y, vi.y, pr));
+          pi = fma(wi.x, vi.y, fma(-wi.y, vi.x, pi));
+        }
       }
       const double dre = block_sum(pr, V.red);
-      const double dim = block_sum(pi, V.red + NW);
-      const double2 al = cmul(make_double2(-0.5 * tau.x, -0.5 * tau.y), make_double2(dre, dim));
-      for (int i = tid; i < m; i += NT) V.w[i] = cfma(al, V.v[i], V.w[i]);
+      const double dim = R ? 0.0 : block_sum(pi, V.red + NW);
+      const double2 al = z_mul<R>(make_double2(-0.5 * tau.x, -0.5 * tau.y), make_double2(dre, dim));
+      for (int i = tid; i < m; i += NT) V.w[i] = z_fma<R>(al, V.v[i], V.w[i]);
       __syncthreads();
-      her2_lower(T, lda, m, V.v, V.w);
+      her2_lower<R>(T, lda, m, V.v, V.w);
       __syncthreads();
       if (tid == 0) x[0] = make_double2(V.sc[0], 0.0);
     } else {
@@ -503,6 +532,9 @@ __device__ void aux_zero_rows(double2* A, int lda, int n) {
   }
 }
 
+// R = true: real arithmetic on the real parts of H and S (problems whose
+// imaginary parts are all zero; the caller routes them).  R = false: complex.
+template <bool R>
 __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const int32_t* __restrict__ nvec,
                                                  const int64_t* __restrict__ hs_off,
                                                  const int64_t* __restrict__ eig_off,
@@ -562,16 +594,16 @@ __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const
     aux_zero_rows(Ha, lda, n);
     aux_zero_rows(Sa, lda, n);
     __syncthreads();
-    const bool ok = cholesky_lower(Sa, lda, n, V);
+    const bool ok = cholesky_lower<R>(Sa, lda, n, V);
     if (!ok) {
       for (int j = tid; j < n; j += NT) eig[eig_off[p] + j] = __longlong_as_double(0x7ff8000000000000LL);
       if (tid == 0) status[p] = SKN_ERR_NOT_SPD;
       __syncthreads();
       continue;
     }
-    hegs2_lower(Ha, lda, Sa, lda, n, V, in_smem ? nullptr : Hs);
     double* tri = tri_all != nullptr ? tri_all + 4 * eig_off[p] : nullptr;
-    hetd2_lower(Ha, lda, n, V, tri);
+    hegs2_lower<R>(Ha, lda, Sa, lda, n, V, in_smem ? nullptr : Hs);
+    hetd2_lower<R>(Ha, lda, n, V, tri);
     if (n == 1 && tid == 0) V.d[0] = Ha[0].x;
     __syncthreads();
     tridiag_eigenvalues(n, V, eig + eig_off[p]);
@@ -826,10 +858,37 @@ static size_t vec_smem_bytes(int mn) {
   return sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;
 }
 static cudaError_t set_smem_limit_once() {
-  cudaError_t e = cudaFuncSetAttribute(k_eigh_gen, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_eigh_gen<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)eig_smem_bytes(MAX_N));
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_eigh_gen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)eig_smem_bytes(MAX_N));
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_eigvec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_smem_bytes(MAX_N));
+}
+
+// Values-only launch of k_eigh_gen<R> over a persistent grid (all problems of the call).
+template <bool R>
+static int launch_values(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
+                         const int32_t* order, double* H, double* S, double* eig, int32_t* status,
+                         int32_t* work_counter, int max_n, cudaStream_t stream) {
+  if (n_prob < 0 || max_n < 0) return SKN_ERR_ARG;
+  if (n_prob == 0) return SKN_OK;
+  if (!n || !hs_off || !eig_off || !order || !H || !S || !eig || !status || !work_counter) return SKN_ERR_ARG;
+  if (max_n > MAX_N) return SKN_ERR_CAPACITY;
+  const int mn = max_n < 1 ? 1 : max_n;
+  const size_t smem = eig_smem_bytes(mn);
+  if (set_smem_limit_once() != cudaSuccess) return SKN_ERR_CUDA;
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigh_gen<R>, NT, smem) != cudaSuccess || per_sm < 1)
+    return SKN_ERR_CUDA;
+  int grid = sms * per_sm;
+  if (grid > n_prob) grid = n_prob;
+  if (cudaMemsetAsync(work_counter, 0, sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
+  k_eigh_gen<R><<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig,
+                                            status, work_counter, mn, 1, nullptr);
+  return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
 }
 
 // A translation unit that includes this file for its kernels alone defines
@@ -838,26 +897,14 @@ static cudaError_t set_smem_limit_once() {
 extern "C" int SKN_EXPORT(skn_eigh_gen_batched)(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
                                     const int32_t* order, double* H, double* S, double* eig, int32_t* status,
                                     int32_t* work_counter, int max_n, cudaStream_t stream) {
-  if (n_prob < 0 || max_n < 0) return SKN_ERR_ARG;
-  if (n_prob == 0) return SKN_OK;
-  if (!n || !hs_off || !eig_off || !order || !H || !S || !eig || !status || !work_counter) return SKN_ERR_ARG;
-  if (max_n > MAX_N) return SKN_ERR_CAPACITY;
-  const int mn = max_n < 1 ? 1 : max_n;
-  const int use_smem_mats = 1;
-  size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn);
-  smem += (size_t)use_smem_mats * SMEM_REGION * sizeof(double2);
-  if (set_smem_limit_once() != cudaSuccess) return SKN_ERR_CUDA;
-  int per_sm = 0, dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigh_gen, NT, smem) != cudaSuccess || per_sm < 1)
-    return SKN_ERR_CUDA;
-  int grid = sms * per_sm;
-  if (grid > n_prob) grid = n_prob;
-  if (cudaMemsetAsync(work_counter, 0, sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
-  k_eigh_gen<<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
-                                         work_counter, mn, use_smem_mats, nullptr);
-  return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
+  return launch_values<false>(n_prob, n, hs_off, eig_off, order, H, S, eig, status, work_counter, max_n, stream);
+}
+
+extern "C" int SKN_EXPORT(skn_eigh_gen_batched_real)(int n_prob, const int32_t* n, const int64_t* hs_off,
+                                                    const int64_t* eig_off, const int32_t* order, double* H,
+                                                    double* S, double* eig, int32_t* status,
+                                                    int32_t* work_counter, int max_n, cudaStream_t stream) {
+  return launch_values<true>(n_prob, n, hs_off, eig_off, order, H, S, eig, status, work_counter, max_n, stream);
 }
 
 static int vec_grid(int n_prob) {
@@ -895,12 +942,13 @@ extern "C" int SKN_EXPORT(skn_eigh_gen_vectors)(int n_prob, const int32_t* n, co
   int per_sm = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigh_gen, NT, smem) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigh_gen<false>, NT, smem) != cudaSuccess ||
+      per_sm < 1)
     return SKN_ERR_CUDA;
   int grid = sms * per_sm;
   if (grid > n_prob) grid = n_prob;
   if (cudaMemsetAsync(work_counter, 0, 2 * sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
-  k_eigh_gen<<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
+  k_eigh_gen<false><<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
                                          work_counter, mn, use_smem_mats, tri);
   if (cudaPeekAtLastError() != cudaSuccess) return SKN_ERR_CUDA;
   const size_t vsmem = sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;

@@ -71,7 +71,8 @@ extern "C" int skn_eigh_gen_vectors_noalloc(int n_prob, const int32_t* n, const 
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t smem = eig_smem_bytes(mn);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigh_gen, NT, smem) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigh_gen<false>, NT, smem) != cudaSuccess ||
+      per_sm < 1)
     return SKN_ERR_CUDA;
   int grid = sms * per_sm;
   if (grid > n_prob) grid = n_prob;
@@ -81,7 +82,7 @@ extern "C" int skn_eigh_gen_vectors_noalloc(int n_prob, const int32_t* n, const 
   if (vgrid > n_prob) vgrid = n_prob;
   // only the queue counters must start at zero; every tri row and scratch entry is written before it is read
   if (cudaMemsetAsync(counter, 0, 2 * sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
-  k_eigh_gen<<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
+  k_eigh_gen<false><<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
                                          counter, mn, use_smem_mats, tri);
   if (cudaPeekAtLastError() != cudaSuccess) return SKN_ERR_CUDA;
   k_eigvec<<<vgrid, VNT, vec_smem_bytes(mn), stream>>>(n_prob, n, hs_off, eig_off, order, (const double2*)H,

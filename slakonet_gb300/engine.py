@@ -193,6 +193,9 @@ class Plan:
     order: np.ndarray
     nelec: np.ndarray
     max_n: int
+    # problems whose H(k), S(k) are exactly real: every component of 2k is an integer, so the
+    # Bloch phases exp(i 2 pi k.T) are exactly +-1
+    prob_real: Optional[np.ndarray] = None
 
 
 def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUTOFF_BOHR) -> Plan:
@@ -258,12 +261,15 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
     eig_off_prob = eig_off_struct[prob_struct] + prob_k.astype(np.int64) * prob_n
     order = np.argsort(-prob_n, kind="stable").astype(np.int32)
     kw_off = k_ptr[:-1].astype(np.int64)
+    kall = np.concatenate(kp) if S else np.zeros((0, 3))
+    prob_real = np.all(2.0 * kall == np.round(2.0 * kall), axis=1)
     return Plan(S, nums, atom_ptr, orb_ptr, np.concatenate(pos), np.stack(cells), np.stack(rng),
                 np.concatenate(species), np.concatenate(norb).astype(np.int32), np.concatenate(aoff),
                 np.concatenate(oatom), np.concatenate(onsite), pair_base, int(pb),
                 np.concatenate(ninj).astype(np.int64), k_ptr, np.concatenate(kp), np.concatenate(kw), kw_off,
                 nk, nb, phase_base, int(phb), prob_struct, prob_k, prob_n, hs_off, int(sz.sum()),
-                eig_off_prob, eig_off_struct, int(eig_sz.sum()), order, nelec, int(nb.max()) if S else 0)
+                eig_off_prob, eig_off_struct, int(eig_sz.sum()), order, nelec, int(nb.max()) if S else 0,
+                prob_real=prob_real)
 
 
 # ------------------------------------------------------------------ engine
@@ -377,7 +383,8 @@ class Engine:
     """Runs the whole path for a planned batch on one CUDA stream."""
 
     def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None,
-                 tuning=None, large_threshold: Optional[int] = 1024, large_cluster: Optional[int] = None):
+                 tuning=None, large_threshold: Optional[int] = 1024, large_cluster: Optional[int] = None,
+                 real_path: bool = True):
         _dev(tables.device)
         self.tables = tables
         self.tuning = tuning          # autotune.Tuning: eigensolver launch shape per problem-size bucket
@@ -385,6 +392,9 @@ class Engine:
         # see route_large (large_cluster None: cluster_for(n))
         self.large_threshold = large_threshold
         self.large_cluster = large_cluster
+        # values-only solves of problems with exactly real H(k), S(k) use the real-arithmetic
+        # kernel (skn_eigh_gen_batched_real): same numbers, a quarter of the FP64 work
+        self.real_path = bool(real_path)
         self.cutoff = float(cutoff)
         self.device = tables.device
         self.stream = stream
@@ -592,7 +602,7 @@ class Engine:
 
         Empty when every problem takes the default single-CTA launch."""
         plan = db.plan
-        key = (id(self.tuning), self.large_threshold, self.large_cluster)
+        key = (id(self.tuning), self.large_threshold, self.large_cluster, self.real_path)
         cache = getattr(db, "_groups", None)
         if cache is not None and cache[0] == key:
             return cache[1]
@@ -605,9 +615,12 @@ class Engine:
         small_order = plan.order[~large]
         if len(small_order):
             if self.tuning is None:
-                shapes = np.array([""] * len(small_order))
+                shapes = [""] * len(small_order)
             else:
-                shapes = np.array([self.tuning.shape_for(int(n)) for n in plan.prob_n[small_order]])
+                shapes = [self.tuning.shape_for(int(n)) for n in plan.prob_n[small_order]]
+            if self.real_path and plan.prob_real is not None:
+                shapes = [("_real" + sh) if r else sh for sh, r in zip(shapes, plan.prob_real[small_order])]
+            shapes = np.array(shapes, dtype=object)
             for sfx in dict.fromkeys(shapes.tolist()):
                 sel = small_order[shapes == sfx]
                 out.append((sfx, _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))

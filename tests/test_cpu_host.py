@@ -135,3 +135,13 @@ def test_large_problem_routing_depends_on_each_problem_alone():
     # no threshold: only problems above the one-CTA bound move; a fixed cluster size overrides
     assert E.route_large(n, None).tolist() == [0, 0, 0, 0, 0, 8, 8, 12, 12]
     assert E.route_large(n, 0, 2).tolist() == [2] * len(n)
+
+
+def test_real_kpoints_marked_in_plan():
+    sd = syn.default_shell_dict()
+    tables = syn.make_tables([14], sd, seed=0)
+    ts = E.TableSet.from_synthetic(tables, {14: sd[14]}, "cpu")
+    st = syn.diamond_si()
+    st["kpoints"] = np.array([[0.0, 0.0, 0.0], [0.5, 0.0, -0.5], [0.25, 0.0, 0.0], [0.5, 1.0 / 3.0, 0.0]])
+    plan = E.plan_batch([st], ts)
+    assert plan.prob_real.tolist() == [True, True, False, False]
