@@ -413,7 +413,8 @@ def run_large_structure(dev):
             "eig_status_ok": int((res.eig_status == 0).sum()), "wall_s": wall,
             "phase_s": {k: round(v, 4) for k, v in phases.items()},
             "eigensolve_tflops": flops / eig_s * 1e-12, "gap_eV": float(res.stats[0, E.STAT["gap_ev"]]),
-            "note": "k-points on 16-CTA cluster eigensolvers (skn_eigh_gen_large), one cluster per k-point"}
+            "note": "k-points on the cluster eigensolver (skn_eigh_gen_large), one cluster of "
+                    f"{E.cluster_for(n)} CTAs per k-point"}
 
 
 def run_cpu_baseline(sts, tables, sd, reps=1):

@@ -261,6 +261,22 @@ int skn_eigh_vectors_scratch_bytes_t64(int n_prob, int max_n, int64_t* bytes);
 int skn_eigh_vectors_scratch_bytes_t256(int n_prob, int max_n, int64_t* bytes);
 
 /*
+ * Atom-type projected DOS of one structure.  Replaces
+ * compute_atom_projected_dos (slakonet/predict_slakonet.py:119-210).
+ *   eig        [nk][nb] eigenvalues, Hartree
+ *   vec        complex [nk][n_orb][nb]: component i of eigenvector b (x^H S x = 1)
+ *   orb_group  [n_orb] atom-type index (0..n_group-1) of each orbital
+ *   fermi_ev   Fermi level (eV); the grid is linspace(e_lo, e_hi, npts) eV relative to it
+ *   sigma      Gaussian width (eV); h2e the Hartree-to-eV factor of the eigenvalues
+ *   weights    scratch: nk * nb * n_group doubles
+ *   grid       out: [npts]; pdos out: [n_group][npts]
+ * pdos[g][e] = (1/nk) sum_{k,b} (sum_{i in g} |c_ib|^2) exp(-((E_e + E_F - e_kb h2e)/sigma)^2 / 2) / (sigma sqrt(2 pi)).
+ */
+int skn_atom_pdos(int nk, int nb, int n_orb, const double* eig, const double* vec, const int32_t* orb_group,
+                  int n_group, double fermi_ev, double e_lo, double e_hi, int npts, double sigma, double h2e,
+                  double* weights, double* grid, double* pdos, cudaStream_t stream);
+
+/*
  * Fermi level, band gap and band-structure statistics per structure.
  * Replaces fermi_search / fermi_dirac (slakonet/fermi.py:139-215),
  * calculate_band_gap (slakonet/main.py:637-707),

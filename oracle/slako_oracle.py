@@ -509,6 +509,47 @@ def gaussian_dos(eig: np.ndarray, weights: np.ndarray, mu: float, energy_range=(
     return grid, dos
 
 
+def atom_projected_dos(eig_ha: np.ndarray, vecs: np.ndarray, atom_types, fermi_ev: float, sigma: float = 0.1,
+                       energy_range=(-8.0, 6.0), n_points: int = 1000):
+    """Atom-type projected DOS, ``compute_atom_projected_dos`` (slakonet/predict_slakonet.py:119-210).
+
+    eig_ha [nk, nb] Hartree; vecs [nk, n_orb, nb] (component, band), the
+    reference's eigenvectors (x^H S x = 1).  The orbitals are split into equal
+    contiguous blocks, one per atom (n_orb must divide by the atom count, as in
+    the reference, whatever each species' real orbital count); an atom type's
+    weight for band b is sum |c_ib|^2 over its blocks.  Each (k, b) adds
+    weight * exp(-0.5 ((E - e_kb) / sigma)^2) / (sigma sqrt(2 pi)) on the grid
+    E = linspace(energy_range) + E_F (eV); the sum is divided by nk.
+    Returns (grid relative to E_F, {type: pdos}, unique types in first-seen order).
+    """
+    eig = np.asarray(eig_ha) * H2E
+    nk, nb = eig.shape
+    grid = torch_linspace(energy_range[0], energy_range[1], n_points)
+    grid_ev = grid + fermi_ev
+    unique = list(dict.fromkeys(atom_types))
+    n_orb = vecs.shape[1]
+    n_atoms = len(atom_types)
+    if n_orb % n_atoms != 0:
+        raise ValueError(f"n_orbitals ({n_orb}) not divisible by n_atoms ({n_atoms}).")
+    per = n_orb // n_atoms
+    idx = {a: [] for a in unique}
+    o = 0
+    for a in atom_types:
+        idx[a].extend(range(o, o + per))
+        o += per
+    norm = 1.0 / (sigma * np.sqrt(2 * np.pi))
+    pdos = {a: np.zeros(n_points) for a in unique}
+    w = {a: (np.abs(vecs[:, idx[a], :]) ** 2).sum(1) for a in unique}   # [nk, nb]
+    for k in range(nk):
+        for b in range(nb):
+            g = norm * np.exp(-0.5 * ((grid_ev - eig[k, b]) / sigma) ** 2)
+            for a in unique:
+                pdos[a] += w[a][k, b] * g
+    for a in unique:
+        pdos[a] /= nk
+    return grid, pdos, unique
+
+
 def properties(eig: np.ndarray, weights: np.ndarray, n_electrons: float,
                dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1) -> dict:
     """The properties dict of ``get_properties_dict`` (slakonet/main.py:1657-1819)

@@ -52,6 +52,7 @@ SIGNATURES = {
     "skn_adj_bloch": [I64] + [P] * 18 + [P],
     "skn_adj_tables": [I64, P, P, P, P, P, P, I32, P, P, P, P, P, P, P, P, P, P, P, P],
     "skn_dos_backward": [I32, P, P, P, P, P, P, P, F64, F64, I32, F64, F64, P, P, I32, P],
+    "skn_atom_pdos": [I32, I32, I32, P, P, P, I32, F64, F64, F64, I32, F64, F64, P, P, P, P],
 }
 for _sfx in ("_t64", "_t256"):
     SIGNATURES["skn_eigh_gen_batched" + _sfx] = SIGNATURES["skn_eigh_gen_batched"]

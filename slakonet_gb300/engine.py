@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import threading
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence
 
@@ -346,6 +347,8 @@ KERNELS_PER_CALL = {"skn_bond_counts": 1, "skn_bond_fill": 1, "skn_image_phases"
                     "skn_bloch": 1, "skn_eigh_gen_batched": 1, "skn_eigh_gen_vectors": 2, "skn_fermi_gap": 1,
                     "skn_dos": 2, "skn_eigh_gen_large": 1, "skn_eigh_gen_vectors_noalloc": 2}
 
+_SIDE = threading.local()   # per-thread side streams of Engine._side_streams
+
 SINGLE_CTA_MAX_N = 2048   # bound of the one-CTA-per-problem eigensolver (csrc/eigh.cu)
 LARGE_MAX_N = 9216        # bound of the cluster eigensolver (csrc/eigh_cluster.cu)
 
@@ -590,10 +593,14 @@ class Engine:
             main.wait_event(ev)
 
     def _side_streams(self, k):
-        cur = getattr(self, "_sides", [])
+        """k side streams for forked launches, cached per host thread and device (engines are
+        created per batch by the server; creating streams per batch would cost more than the fork)."""
+        pool = getattr(_SIDE, "pool", None)
+        if pool is None:
+            pool = _SIDE.pool = {}
+        cur = pool.setdefault(self.device.index if self.device.index is not None else 0, [])
         while len(cur) < k:
             cur.append(torch.cuda.Stream(self.device))
-        self._sides = cur
         return cur
 
     def _groups(self, db):

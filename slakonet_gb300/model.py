@@ -50,6 +50,12 @@ class Geometry:
     def n_atoms(self):
         return self.atomic_numbers.count_nonzero(-1)
 
+    @property
+    def chemical_symbols(self) -> list:
+        """Chemical symbols per batch entry, as ``Geometry.chemical_symbols`` (slakonet/atoms.py:751-754)."""
+        from .elements import SYMBOLS
+        return [[SYMBOLS[int(z)] for z in row if int(z) != 0] for row in self.atomic_numbers.tolist()]
+
 
 def _structure_from_geometry(geometry) -> dict:
     z = torch.as_tensor(geometry.atomic_numbers).detach().cpu().reshape(-1).numpy()
@@ -274,7 +280,10 @@ class MultiElementSkfParameterOptimizer(nn.Module):
         st["kpoints"] = k
         st["weights"] = np.full(len(k), 1.0 / len(k))
         res = self.compute_properties_batch([st], shell_dict, device, with_eigenvectors=with_eigenvectors)
-        return properties_dict(res, 0, get_fermi=get_fermi), True
+        props = properties_dict(res, 0, get_fermi=get_fermi)
+        if "calc" in props:
+            props["calc"].geometry = geometry     # as the reference's calculator (SimpleDftb.geometry)
+        return props, True
 
 
 def _default_shell_dict():

@@ -117,6 +117,32 @@ def run_reference(model, st, shell_dict, kpoints=None, mesh=None, klines=None, k
     return out
 
 
+def fixture_pdos(name, st, shell_dict, table_seed, mesh, energy_range=(-10.0, 10.0)):
+    """Atom-type projected DOS from the reference's own ``compute_atom_projected_dos``
+    (slakonet/predict_slakonet.py:119-210) on its eigenvectors (with_eigenvectors=True)."""
+    zs = sorted({int(z) for z in st["numbers"]})
+    tables = syn.make_tables(zs, syn.default_shell_dict() if shell_dict is None else shell_dict, seed=table_seed)
+    sd = {z: (shell_dict or syn.default_shell_dict())[z] for z in zs}
+    model = build_reference_model(ref, tables)
+    geom = geometry(st)
+    with torch.no_grad():
+        props, ok = model.compute_multi_element_properties(geometry=geom, shell_dict=sd, kpoints=torch.tensor(mesh),
+                                                           device="cpu", get_fermi=True, with_eigenvectors=True)
+        grid, pdos, unique = ref.predict.compute_atom_projected_dos(props, geom, sigma=0.1,
+                                                                    energy_range=energy_range)
+    calc = props["calc"]
+    payload = dict(numbers=st["numbers"], positions=st["positions"], cell=st["cell"], mesh=np.array(mesh),
+                   table_seed=table_seed, tables_checksum=tables_checksum(tables),
+                   shells=np.array([len(sd[z]) for z in zs]), shell_z=np.array(zs),
+                   energy_range=np.array(energy_range), fermi_energy_eV=float(props["fermi_energy_eV"]),
+                   eigenvalues=calc.eigenvalue[0].numpy(),
+                   eigenvectors=calc.eigenvectors[0].permute(2, 0, 1).numpy(),   # [nk, component, band]
+                   grid=grid, unique=np.array(unique),
+                   pdos=np.stack([pdos[a] for a in unique]))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **payload)
+    print(name, "pdos", {a: float(np.trapezoid(pdos[a], grid)) for a in unique})
+
+
 def fixture_interp():
     rng = np.random.default_rng(11)
     grid = syn.grid_points()
@@ -305,9 +331,25 @@ def fixture_gradients():
             print("  ", f[0], f[1], f"{f[2]: .6e} {f[3]: .6e} {f[4]: .6e}")
 
 
+def fixtures_pdos():
+    si = syn.diamond_si()
+    fixture_pdos("pdos_si", si, {14: [0, 1, 2]}, 0, (3, 3, 3))
+    a = 5.65 * syn.ANGSTROM_TO_BOHR
+    gaas = {"numbers": np.array([31, 33]), "positions": np.array([[0.0, 0.0, 0.0], [0.25 * a] * 3]),
+            "cell": 0.5 * a * np.array([[0.0, 1.0, 1.0], [1.0, 0.0, 1.0], [1.0, 1.0, 0.0]])}
+    fixture_pdos("pdos_gaas", gaas, None, 1, (3, 3, 3))
+    # H (1 orbital) and Fe (9): 10 orbitals over 2 atoms; the reference splits them into equal blocks of 5
+    hfe = {"numbers": np.array([1, 26]), "positions": np.array([[0.0, 0.0, 0.0], [1.6, 1.6, 1.6]]),
+           "cell": np.eye(3) * 5.4}
+    fixture_pdos("pdos_hfe", hfe, None, 2, (2, 2, 2))
+
+
 if __name__ == "__main__":
     if "--gradients-only" in sys.argv:
         fixture_gradients()
+        sys.exit(0)
+    if "--pdos-only" in sys.argv:
+        fixtures_pdos()
         sys.exit(0)
     fixture_interp()
     fixture_blocks()
@@ -319,4 +361,5 @@ if __name__ == "__main__":
     fixture_random("rand_b", 9, 22, 22)
     fixture_random("rand_c", 3, 23, 23)
     fixture_gradients()
+    fixtures_pdos()
     print("golden fixtures written to", HERE)

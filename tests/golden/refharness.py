@@ -49,6 +49,10 @@ def _install_stubs():
     mpl.use = lambda *a, **k: None
     plt = mod("matplotlib.pyplot")
     mpl.pyplot = plt
+    plt.rcParams = {}
+    gs = mod("matplotlib.gridspec")
+    gs.GridSpec = _Anything
+    mpl.gridspec = gs
     for nm in ("figure", "plot", "savefig", "close", "subplots", "xlabel", "ylabel",
                "legend", "tight_layout", "title", "xlim", "ylim", "axhline", "axvline"):
         setattr(plt, nm, lambda *a, **k: _Anything())
@@ -67,6 +71,8 @@ def _install_stubs():
     vasp = mod("jarvis.io.vasp")
     outs = mod("jarvis.io.vasp.outputs")
     outs.Vasprun = _Anything
+    inputs = mod("jarvis.io.vasp.inputs")
+    inputs.Poscar = _Anything
 
     def atomic_numbers_to_symbols(zz):
         from slakonet.elements import chemical_symbols
@@ -88,8 +94,9 @@ def import_reference():
     import slakonet.interpolation as interp
     import slakonet.fermi as fermi
     import slakonet.utils as utils
+    import slakonet.predict_slakonet as predict
     return types.SimpleNamespace(optim=optim, main=main, skf=skf, atoms=atoms,
-                                 sk=sk, interp=interp, fermi=fermi, utils=utils)
+                                 sk=sk, interp=interp, fermi=fermi, utils=utils, predict=predict)
 
 
 def build_reference_model(ref, tables):

@@ -82,3 +82,23 @@ def test_kpoint_generators():
     g = golden("si_klines")
     k, w = O.klines_kpoints(g["klines"])
     assert np.abs(k - g["kpoints"]).max() <= 1e-15
+
+
+@pytest.mark.parametrize("name", ["pdos_si", "pdos_gaas", "pdos_hfe"])
+def test_oracle_atom_projected_dos_matches_reference(name):
+    """The restatement on the reference's own eigenvectors reproduces its PDOS."""
+    g = golden(name)
+    from slakonet_gb300.elements import SYMBOLS
+    types = [SYMBOLS[int(z)] for z in g["numbers"]]
+    grid, pdos, unique = O.atom_projected_dos(g["eigenvalues"], g["eigenvectors"], types,
+                                              float(g["fermi_energy_eV"]), 0.1, tuple(g["energy_range"]))
+    assert unique == [str(u) for u in g["unique"]]
+    np.testing.assert_array_equal(grid, g["grid"])
+    err = max(np.abs(pdos[a] - g["pdos"][i]).max() for i, a in enumerate(unique))
+    print(f"{name}: oracle PDOS vs reference {err:.1e}")
+    assert err <= 1e-12
+
+
+def test_oracle_atom_projected_dos_refuses_indivisible_orbitals():
+    with pytest.raises(ValueError):
+        O.atom_projected_dos(np.zeros((1, 5)), np.zeros((1, 5, 5)), ["H", "C"], 0.0)
