@@ -550,6 +550,40 @@ def atom_projected_dos(eig_ha: np.ndarray, vecs: np.ndarray, atom_types, fermi_e
     return grid, pdos, unique
 
 
+def band_energy(eig: np.ndarray, weights: np.ndarray, mu: float, kT_ev: float = 0.025) -> float:
+    """Fermi-smeared band energy, ``SimpleDftb._calculate_electronic_energy`` (slakonet/main.py:1430-1448):
+    sum_k w_k sum_b f(e_kb) e_kb with f = 1 / (1 + exp((e - mu) / kT)), kT = 0.025 eV, and f = 0
+    where e is exactly zero (``fermi_smearing``, slakonet/fermi.py:54-96).  Hartree."""
+    kT = kT_ev / H2E
+    with np.errstate(over="ignore"):
+        occ = 1.0 / (1.0 + np.exp((eig - mu) / kT))
+    occ[eig == 0] = 0.0
+    return float(np.sum(occ * eig * np.asarray(weights)[:, None]))
+
+
+def fd_forces(structure: dict, tables: dict, shell_dict, delta: float = 1e-2, mesh=(5, 5, 5)) -> np.ndarray:
+    """``_compute_forces_finite_diff`` (slakonet/main.py:198-281): F_ij = -(E(+) - E(-)) / (2 delta), with E
+    the plain sum of every eigenvalue (no weights, no occupations) on a ``mesh`` Monkhorst-Pack grid and
+    the atom displaced by +-delta Bohr along axis j."""
+    k, _ = mp_kpoints(mesh)
+    pos = np.asarray(structure["positions"], dtype=np.float64)
+    F = np.zeros_like(pos)
+
+    def energy(p):
+        st = dict(structure, positions=p)
+        H, S = hk_sk(st, tables, shell_dict, k)
+        return float(sum(np.sum(eigh_generalized(H[q], S[q])) for q in range(len(k))))
+
+    for i in range(pos.shape[0]):
+        for j in range(3):
+            pf = pos.copy()
+            pf[i, j] += delta
+            pb = pos.copy()
+            pb[i, j] -= delta
+            F[i, j] = -(energy(pf) - energy(pb)) / (2 * delta)
+    return F
+
+
 def properties(eig: np.ndarray, weights: np.ndarray, n_electrons: float,
                dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1) -> dict:
     """The properties dict of ``get_properties_dict`` (slakonet/main.py:1657-1819)

@@ -31,7 +31,8 @@ enum {
   ST_MU_HA = 0, ST_FERMI_EV = 1, ST_GAP_EV = 2, ST_VBM_EV = 3, ST_CBM_EV = 4, ST_DIRECT = 5,
   ST_VBM_K = 6, ST_CBM_K = 7, ST_VWIDTH = 8, ST_CWIDTH = 9, ST_MIN_DGAP = 10, ST_DIRECT_SEMI = 11,
   ST_EFERMI_EV = 12, ST_BANDGAP_EV = 13, ST_CONVERGED = 14, ST_ITERS = 15, ST_DOS_FERMI = 16,
-  ST_DOS_GAPC = 17, ST_DOS_TOTAL = 18, ST_METAL = 19, ST_FALLBACK = 20, ST_VBM_FLAT = 21, ST_CBM_FLAT = 22
+  ST_DOS_GAPC = 17, ST_DOS_TOTAL = 18, ST_METAL = 19, ST_FALLBACK = 20, ST_VBM_FLAT = 21, ST_CBM_FLAT = 22,
+  ST_BAND_ENERGY = 23
 };
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }
@@ -111,6 +112,20 @@ __global__ void __launch_bounds__(NT) k_fermi_gap(const int64_t* __restrict__ ei
     const double grad = (2.0 * (2.0 * diff)) * sumg / kT;
     if (fabs(grad) < tol) { iters = it; conv = 1; break; }
     mu = mu - loss / (grad + 1e-12);
+  }
+
+  // Fermi-smeared band energy, SimpleDftb._calculate_electronic_energy (slakonet/main.py:1430-1448):
+  // sum_k w_k sum_b f(e_kb; mu, 0.025 eV) e_kb, with f = 0 where e_kb is exactly zero (fermi_smearing,
+  // slakonet/fermi.py:54-96)
+  {
+    const double kT_e = 0.025 / H2E;
+    double be = 0.0, unused = 0.0;
+    for (int e = tid; e < tot; e += NT) {
+      const double occ = (E[e] == 0.0) ? 0.0 : 1.0 / (1.0 + exp((E[e] - mu) / kT_e));
+      be += (occ * E[e]) * w[e / nb];
+    }
+    block_sum2(be, unused, red);
+    if (tid == 0) st[ST_BAND_ENERGY] = be;
   }
 
   // calculate_band_gap

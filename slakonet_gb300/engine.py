@@ -30,7 +30,8 @@ KT_FERMI = 0.01             # fermi_search default (slakonet/fermi.py:143)
 # stats record layout (mirrors csrc/fermi_dos.cu)
 STAT = dict(mu_ha=0, fermi_ev=1, gap_ev=2, vbm_ev=3, cbm_ev=4, direct=5, vbm_k=6, cbm_k=7, vwidth=8,
             cwidth=9, min_dgap=10, direct_semi=11, efermi_ev=12, bandgap_ev=13, converged=14, iters=15,
-            dos_fermi=16, dos_gapc=17, dos_total=18, metal=19, fallback=20, vbm_flat=21, cbm_flat=22)
+            dos_fermi=16, dos_gapc=17, dos_total=18, metal=19, fallback=20, vbm_flat=21, cbm_flat=22,
+            band_energy_ha=23)
 
 
 def _dev(device) -> torch.device:

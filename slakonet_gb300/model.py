@@ -13,6 +13,9 @@ slakonet/main.py:1657-1819); the numbers come from the CUDA path in
 """
 from __future__ import annotations
 
+import os
+import re
+
 import types
 from typing import Dict, List, Optional, Sequence
 
@@ -162,6 +165,45 @@ class MultiElementSkfParameterOptimizer(nn.Module):
         return m
 
     @classmethod
+    def from_skf_files(cls, files) -> "MultiElementSkfParameterOptimizer":
+        """From DFTB+ Slater-Koster files: a directory of ``A-B.skf`` files, or a dict
+        ``{(za, zb) or "A-B": path}``.  Every ordered pair needs its file (A-B and B-A), and
+        every element its A-A file (on-site energies, occupations).  See ``slakonet_gb300.skf``."""
+        from . import skf as SKF
+        if isinstance(files, (str, os.PathLike)):
+            found = {}
+            for name in sorted(os.listdir(files)):
+                m_ = re.fullmatch(r"([A-Z][a-z]?)-([A-Z][a-z]?)\.skf", name)
+                if m_:
+                    found[(SYMBOLS.index(m_.group(1)), SYMBOLS.index(m_.group(2)))] = os.path.join(files, name)
+            files = found
+        m = cls()
+        for key, path in sorted(((k if isinstance(k, tuple) else tuple(SYMBOLS.index(x) for x in k.split("-"))), v)
+                                for k, v in files.items()):
+            za, zb = int(key[0]), int(key[1])
+            d = SKF.read_skf(path, homonuclear=(za == zb))
+            h = {f"{l1}-{l2}": v for (l1, l2), v in d["H"].items()}
+            s_ = {f"{l1}-{l2}": v for (l1, l2), v in d["S"].items()}
+            atomic = None
+            if za == zb:
+                a = d["atomic"]
+                atomic = {"on_sites": [float(x) for x in a["on_sites"]],
+                          "hubbard_us": [float(x) for x in a["hubbard_us"]], "mass": float(a["mass"]),
+                          "occupations": [float(x) for x in a["occupations"]]}
+            grid = SKF.grid_from_step(d["grid_step"], d["n_grid"])
+            m.skf_optimizers[f"{SYMBOLS[za]}-{SYMBOLS[zb]}"] = SkfParameterOptimizer((za, zb), h, s_, grid, atomic)
+        return m
+
+    def write_skf_files(self, directory: str):
+        """Write every pair's current parameters as ``A-B.skf`` (DFTB+ v1.0 format)."""
+        from . import skf as SKF
+        os.makedirs(directory, exist_ok=True)
+        for key, opt in self.skf_optimizers.items():
+            H = {tuple(int(x) for x in k.split("-")): v.detach().cpu().numpy() for k, v in opt.h_params.items()}
+            S = {tuple(int(x) for x in k.split("-")): v.detach().cpu().numpy() for k, v in opt.s_params.items()}
+            SKF.write_skf(os.path.join(directory, f"{key}.skf"), H, S, opt.grid_step, opt.atomic_data)
+
+    @classmethod
     def load_ultra_compact(cls, path: str) -> "MultiElementSkfParameterOptimizer":
         """Read the reference's ultra-compact checkpoint (slakonet/optim.py:528-625).
 
@@ -264,8 +306,8 @@ class MultiElementSkfParameterOptimizer(nn.Module):
                                          phonons=False, get_fermi=False, get_energy=False, get_forces=False,
                                          get_bulk_mod=False, device=None, with_eigenvectors=False):
         """Reference signature (slakonet/optim.py:949-962); returns ``(properties, True)``."""
-        if phonons or get_energy or get_forces or get_bulk_mod:
-            raise NotImplementedError("phonons, total energy, forces and bulk modulus are outside this path")
+        if phonons or get_bulk_mod:
+            raise NotImplementedError("phonons and the bulk modulus are outside this path")
         if device is None:
             device = "cuda"
         device = torch.device(device)
@@ -283,7 +325,34 @@ class MultiElementSkfParameterOptimizer(nn.Module):
         props = properties_dict(res, 0, get_fermi=get_fermi)
         if "calc" in props:
             props["calc"].geometry = geometry     # as the reference's calculator (SimpleDftb.geometry)
+        if get_energy:      # slakonet/optim.py:1066-1068
+            props["total_energy"] = res.stats[0, E.STAT["band_energy_ha"]]
+        if get_forces:      # slakonet/optim.py:1069-1071
+            props["forces"] = self.finite_difference_forces(st, shell_dict, device)
         return props, True
+
+    def finite_difference_forces(self, structure: dict, shell_dict=None, device=None, delta: float = 1e-2,
+                                 mesh=(5, 5, 5)) -> torch.Tensor:
+        """Forces as ``SimpleDftb._compute_forces_finite_diff`` (slakonet/main.py:198-281):
+        F_ij = -(E(+) - E(-)) / (2 delta), E the plain sum of every eigenvalue on a ``mesh``
+        Monkhorst-Pack grid, atom i displaced by +-delta Bohr along axis j.  The reference
+        runs the 6N displaced structures one after another; here all of them (6N x nk
+        problems) go through the path as one batch.  Returns [1, N, 3] (Hartree/Bohr)."""
+        device = torch.device(device if device is not None else "cuda")
+        pos = np.asarray(structure["positions"], dtype=np.float64).reshape(-1, 3)
+        k = mp_kpoints(mesh)
+        displaced = []
+        for i in range(len(pos)):
+            for j in range(3):
+                for sgn in (1.0, -1.0):
+                    p = pos.copy()
+                    p[i, j] += sgn * delta
+                    displaced.append({"numbers": structure["numbers"], "positions": p, "cell": structure["cell"],
+                                      "kpoints": k})
+        res = self.compute_properties_batch(displaced, shell_dict, device, dos_points=1)
+        per = int(res.plan.nk[0]) * int(res.plan.nb[0])
+        sums = res.eig[: len(displaced) * per].view(len(displaced), per).sum(1).view(len(pos), 3, 2)
+        return (-(sums[..., 0] - sums[..., 1]) / (2.0 * delta)).unsqueeze(0)
 
 
 def _default_shell_dict():

@@ -331,6 +331,39 @@ def fixture_gradients():
             print("  ", f[0], f[1], f"{f[2]: .6e} {f[3]: .6e} {f[4]: .6e}")
 
 
+def fixture_energy_forces(name, st, shell_dict, table_seed, mesh):
+    """get_energy / get_forces of compute_multi_element_properties (slakonet/optim.py:1066-1071):
+    Fermi-smeared band energy (slakonet/main.py:1430-1448) and central-difference forces on the
+    sum of eigenvalues at a 5x5x5 grid, delta = 0.01 Bohr (slakonet/main.py:198-281)."""
+    zs = sorted({int(z) for z in st["numbers"]})
+    full = syn.default_shell_dict()
+    sd = {z: (shell_dict or full)[z] for z in zs}
+    tables = syn.make_tables(zs, shell_dict or full, seed=table_seed)
+    model = build_reference_model(ref, tables)
+    geom = geometry(st)
+    with torch.no_grad():
+        props, ok = model.compute_multi_element_properties(geometry=geom, shell_dict=sd, kpoints=torch.tensor(mesh),
+                                                           device="cpu", get_fermi=True, get_energy=True,
+                                                           get_forces=True)
+    payload = dict(numbers=st["numbers"], positions=st["positions"], cell=st["cell"], mesh=np.array(mesh),
+                   table_seed=table_seed, tables_checksum=tables_checksum(tables), shell_z=np.array(zs),
+                   shells=np.array([len(sd[z]) for z in zs]),
+                   fermi_energy_Ha=float(props["fermi_energy_Ha"]),
+                   eigenvalues=props["eigenvalues"][0].numpy(), k_weights=props["calc"].k_weights[0].numpy(),
+                   total_energy=float(props["total_energy"]), forces=props["forces"][0].detach().numpy())
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **payload)
+    print(name, "E", payload["total_energy"], "F", payload["forces"].round(6).tolist())
+
+
+def fixtures_energy_forces():
+    rng = np.random.default_rng(31)
+    si = syn.diamond_si()
+    si["positions"] = si["positions"] + rng.normal(0.0, 0.08, si["positions"].shape)
+    fixture_energy_forces("ef_si", si, {14: [0, 1, 2]}, 0, (2, 2, 2))
+    st = syn.random_structure(np.random.default_rng(32), 3, zmax=30)
+    fixture_energy_forces("ef_rand", st, None, 4, (2, 2, 1))
+
+
 def fixtures_pdos():
     si = syn.diamond_si()
     fixture_pdos("pdos_si", si, {14: [0, 1, 2]}, 0, (3, 3, 3))
@@ -351,6 +384,9 @@ if __name__ == "__main__":
     if "--pdos-only" in sys.argv:
         fixtures_pdos()
         sys.exit(0)
+    if "--energy-forces-only" in sys.argv:
+        fixtures_energy_forces()
+        sys.exit(0)
     fixture_interp()
     fixture_blocks()
     fixture_fermi()
@@ -362,4 +398,5 @@ if __name__ == "__main__":
     fixture_random("rand_c", 3, 23, 23)
     fixture_gradients()
     fixtures_pdos()
+    fixtures_energy_forces()
     print("golden fixtures written to", HERE)

@@ -3,7 +3,8 @@ import numpy as np
 import pytest
 
 from conftest import golden
-from _cases import CASES, load_case
+from _cases import CASES, load_case, tables_checksum
+from slakonet_gb300 import synthetic as syn
 from oracle import slako_oracle as O
 
 H2E = 27.211
@@ -102,3 +103,34 @@ def test_oracle_atom_projected_dos_matches_reference(name):
 def test_oracle_atom_projected_dos_refuses_indivisible_orbitals():
     with pytest.raises(ValueError):
         O.atom_projected_dos(np.zeros((1, 5)), np.zeros((1, 5, 5)), ["H", "C"], 0.0)
+
+
+def _ef_case(name):
+    g = golden(name)
+    zs = [int(z) for z in g["shell_z"]]
+    full = syn.default_shell_dict()
+    if name == "ef_si":
+        sd = {14: [0, 1, 2]}
+        tables = syn.make_tables(zs, sd, seed=int(g["table_seed"]))
+    else:
+        tables = syn.make_tables(zs, full, seed=int(g["table_seed"]))
+        sd = {z: full[z] for z in zs}
+    np.testing.assert_allclose(tables_checksum(tables), g["tables_checksum"], rtol=1e-12, atol=1e-300)
+    st = {"numbers": g["numbers"], "positions": g["positions"], "cell": g["cell"]}
+    return g, st, tables, sd
+
+
+@pytest.mark.parametrize("name", ["ef_si", "ef_rand"])
+def test_oracle_band_energy_matches_reference(name):
+    g, st, tables, sd = _ef_case(name)
+    e = O.band_energy(g["eigenvalues"], g["k_weights"], float(g["fermi_energy_Ha"]))
+    print(f"{name}: band energy {e:.15f} vs reference {float(g['total_energy']):.15f}")
+    assert abs(e - float(g["total_energy"])) <= 1e-12 * max(1.0, abs(e))
+
+
+def test_oracle_finite_difference_forces_match_reference():
+    g, st, tables, sd = _ef_case("ef_si")
+    F = O.fd_forces(st, tables, sd)
+    err = np.abs(F - g["forces"]).max()
+    print(f"ef_si: oracle forces vs reference {err:.1e} (max |F| {np.abs(g['forces']).max():.3f})")
+    assert err <= 1e-8
