@@ -13,6 +13,8 @@ slakonet/main.py:1657-1819); the numbers come from the CUDA path in
 """
 from __future__ import annotations
 
+import itertools
+import operator
 import os
 import re
 
@@ -95,15 +97,48 @@ def klines_kpoints(klines) -> np.ndarray:
     return np.array(pts, dtype=np.float64).reshape(-1, 3)
 
 
+# Parameter values reach the device tables through MultiElementSkfParameterOptimizer.table_set,
+# which repacks only when a parameter changed.  Changes are seen through the tensors' version
+# counters (in-place updates under no_grad, optimizer steps, load_state_dict, apply_constraints)
+# and, for the set of parameters itself, through this epoch, bumped whenever a parameter
+# container or entry is replaced.  Assigning ``p.data`` directly bypasses both: call
+# ``invalidate_tables()`` after doing so.
+_PARAM_EPOCH = [0]
+
+
+def _bump_epoch():
+    _PARAM_EPOCH[0] += 1
+
+
+class _TrackedParameterDict(nn.ParameterDict):
+    def __setitem__(self, key, value):
+        super().__setitem__(key, value)
+        _bump_epoch()
+
+    def __delitem__(self, key):
+        super().__delitem__(key)
+        _bump_epoch()
+
+
+class _TrackedModuleDict(nn.ModuleDict):
+    def __setitem__(self, key, module):
+        super().__setitem__(key, module)
+        _bump_epoch()
+
+    def __delitem__(self, key):
+        super().__delitem__(key)
+        _bump_epoch()
+
+
 class SkfParameterOptimizer(nn.Module):
     """Trainable tables of one element pair (slakonet/optim.py:1356-1443)."""
 
     def __init__(self, atom_pair: Sequence[int], h: Dict[str, torch.Tensor], s: Dict[str, torch.Tensor],
                  grid, atomic_data: Optional[dict] = None, hs_cutoff=None):
         super().__init__()
-        self.h_params = nn.ParameterDict({k: nn.Parameter(torch.as_tensor(v, dtype=torch.float64).clone())
+        self.h_params = _TrackedParameterDict({k: nn.Parameter(torch.as_tensor(v, dtype=torch.float64).clone())
                                           for k, v in h.items()})
-        self.s_params = nn.ParameterDict({k: nn.Parameter(torch.as_tensor(v, dtype=torch.float64).clone())
+        self.s_params = _TrackedParameterDict({k: nn.Parameter(torch.as_tensor(v, dtype=torch.float64).clone())
                                           for k, v in s.items()})
         self.original_h_params = {k: v.detach().clone() for k, v in self.h_params.items()}
         self.original_s_params = {k: v.detach().clone() for k, v in self.s_params.items()}
@@ -116,25 +151,30 @@ class SkfParameterOptimizer(nn.Module):
         if atomic_data is not None:
             self.skf_dict["atomic_data"] = atomic_data
 
+    def __setattr__(self, name, value):
+        super().__setattr__(name, value)
+        if name in ("h_params", "s_params"):
+            _bump_epoch()
+
     @property
     def grid_step(self) -> float:
         return self.grid[1] - self.grid[0]
 
     def apply_constraints(self, c=(0.9, 0.7, 0.95, 0.9)):
         """Clamp parameters to a band around their initial values (slakonet/optim.py:1392-1434)."""
+        # same bounds as the reference, applied in place (which the table cache sees)
         with torch.no_grad():
             for key, p in self.h_params.items():
                 o = self.original_h_params[key].to(p.device)
                 f = c[0] if key.split("-")[0] == key.split("-")[1] else c[1]
-                p.data = torch.clamp(p.data, o * f, o * (1 + (1 - f)))
+                p.copy_(torch.clamp(p, o * f, o * (1 + (1 - f))))
             for key, p in self.s_params.items():
                 o = self.original_s_params[key].to(p.device)
                 if key.split("-")[0] == key.split("-")[1]:
-                    p.data = torch.clamp(p.data, torch.maximum(o * c[2], torch.tensor(0.1, dtype=o.dtype,
-                                                                                     device=o.device)),
-                                         o * (1 + (1 - c[2])))
+                    p.copy_(torch.clamp(p, torch.maximum(o * c[2], torch.tensor(0.1, dtype=o.dtype, device=o.device)),
+                                        o * (1 + (1 - c[2]))))
                 else:
-                    p.data = torch.clamp(p.data, o * c[3], o * (1 + (1 - c[3])))
+                    p.copy_(torch.clamp(p, o * c[3], o * (1 + (1 - c[3]))))
 
 
 class MultiElementSkfParameterOptimizer(nn.Module):
@@ -142,9 +182,10 @@ class MultiElementSkfParameterOptimizer(nn.Module):
 
     def __init__(self):
         super().__init__()
-        self.skf_optimizers = nn.ModuleDict()
+        self.skf_optimizers = _TrackedModuleDict()
         self.atomic_num_to_symbol = {z: SYMBOLS[z] for z in range(1, len(SYMBOLS))}
         self._table_cache = None
+        self.__dict__["_invalidations"] = 0
 
     # ------------------------------------------------------------ building
     @classmethod
@@ -242,12 +283,24 @@ class MultiElementSkfParameterOptimizer(nn.Module):
             opt.apply_constraints()
 
     # ------------------------------------------------------------- feeding
+    def __setattr__(self, name, value):
+        super().__setattr__(name, value)
+        if name == "skf_optimizers":
+            _bump_epoch()
+
     def _param_signature(self, device):
-        sig = [str(device)]
-        for key, opt in self.skf_optimizers.items():
-            for p in list(opt.h_params.values()) + list(opt.s_params.values()):
-                sig.append((id(p), p._version, p.data_ptr()))
-        return tuple(sig)
+        cached = self.__dict__.get("_plist")
+        if cached is None or cached[0] != _PARAM_EPOCH[0] or cached[1] != self._invalidations:
+            plist = [p for opt in self.skf_optimizers.values()
+                     for p in itertools.chain(opt.h_params.values(), opt.s_params.values())]
+            cached = (_PARAM_EPOCH[0], self._invalidations, plist)
+            self.__dict__["_plist"] = cached
+        # version counters only grow, so their sum changes whenever any of them does
+        return (str(device), cached[0], cached[1], sum(map(operator.attrgetter("_version"), cached[2])))
+
+    def invalidate_tables(self):
+        """Repack the device tables on the next call (needed only after assigning ``p.data`` directly)."""
+        self.__dict__["_invalidations"] = self._invalidations + 1
 
     def table_set(self, shell_dict: Dict[int, List[int]], device, species: Optional[Sequence[int]] = None):
         """Packed device tables for ``species`` (all elements of the model by default), cached."""

@@ -145,3 +145,28 @@ def test_real_kpoints_marked_in_plan():
     st["kpoints"] = np.array([[0.0, 0.0, 0.0], [0.5, 0.0, -0.5], [0.25, 0.0, 0.0], [0.5, 1.0 / 3.0, 0.0]])
     plan = E.plan_batch([st], ts)
     assert plan.prob_real.tolist() == [True, True, False, False]
+
+
+def test_device_tables_repack_exactly_when_parameters_change():
+    sd = {6: [0, 1], 14: [0, 1, 2]}
+    model = M.MultiElementSkfParameterOptimizer.from_tables(syn.make_tables([6, 14], sd, seed=1))
+    ts = model.table_set(sd, "cpu")
+    assert model.table_set(sd, "cpu") is ts                       # nothing changed: cached
+    opt = model.skf_optimizers["C-Si"]
+    key = next(iter(opt.h_params))
+    import torch
+    with torch.no_grad():
+        opt.h_params[key].mul_(1.01)                               # in-place update (optimizer-style)
+    ts2 = model.table_set(sd, "cpu")
+    assert ts2 is not ts
+    assert model.table_set(sd, "cpu") is ts2
+    opt.apply_constraints()                                        # the reference's clamp, applied in place
+    ts3 = model.table_set(sd, "cpu")
+    assert ts3 is not ts2
+    opt.h_params[key] = torch.nn.Parameter(opt.h_params[key].detach() * 1.0)   # entry replaced
+    ts4 = model.table_set(sd, "cpu")
+    assert ts4 is not ts3
+    opt.h_params[key].data = opt.h_params[key].data * 2.0         # .data assignment is not tracked ...
+    assert model.table_set(sd, "cpu") is ts4
+    model.invalidate_tables()                                      # ... until invalidated
+    assert model.table_set(sd, "cpu") is not ts4
