@@ -348,7 +348,9 @@ def run_training_step(dev, steps=3):
 
 
 def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40):
-    """Config-4-like Poisson stream: 1-200 atoms (log-uniform), Z 1-65, ~1000 k-atoms per structure."""
+    """Config-4 shape: Poisson stream of ``n_requests`` at ``rate`` per second, structures of 1-200 atoms
+    (log-uniform), Z 1-65, ~1000 k-atoms each; then the same requests submitted at once (capacity);
+    then a one-request-at-a-time baseline through the same API."""
     import torch
     from slakonet_gb300 import model as M, serving as SV, synthetic as syn
     sts = syn.uneven_batch(n_requests, nmin=1, nmax=200, zmax=65, seed=SEED + 7)
@@ -362,6 +364,7 @@ def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40):
     SV.poisson_stream(server, sts[:8], rate=1000.0, seed=1)          # warm-up
     lat, wall, res = SV.poisson_stream(server, sts, rate=rate, seed=2)
     batches = server.batches
+    lat_b, wall_b, _ = SV.poisson_stream(server, sts, rate=1e9, seed=3)   # everything at once
     server.close()
     # one request at a time through the same API (no batching, no overlap)
     seq = []
@@ -377,6 +380,8 @@ def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40):
             "p99_ms": 1e3 * float(np.percentile(lat, 99)), "structures_per_s": len(lat) / wall,
             "k_point_solves_per_s": sum(nk) / wall, "batches": batches,
             "rejected": sum(1 for r in res if "error" in r),
+            "capacity": {"structures_per_s": len(lat_b) / wall_b, "k_point_solves_per_s": sum(nk) / wall_b,
+                         "note": "the same requests submitted at once"},
             "sequential_baseline": {"sample": seq_sample, "p50_ms": 1e3 * float(np.median(seq)),
                                     "structures_per_s": seq_sample / sum(seq)},
             "workload": "Poisson arrivals; structures 1-200 atoms log-uniform, Z=1-65, Gamma-centred ~1000 k-atoms; "
@@ -472,6 +477,8 @@ def main():
     ap.add_argument("--seed", type=int, default=SEED)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the training-step and serving measurements")
+    ap.add_argument("--serving-requests", type=int, default=200, help="requests in the serving stream")
+    ap.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream (1/s)")
     ap.add_argument("--large-structure", action="store_true",
                     help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
     args = ap.parse_args()
@@ -493,7 +500,7 @@ def main():
             log("training step")
             out["training_step"] = run_training_step(dev)
             log("serving")
-            out["serving"] = run_serving(dev)
+            out["serving"] = run_serving(dev, args.serving_requests, args.serving_rate)
         if world == 1 and args.large_structure:
             import torch
             log("large structure")

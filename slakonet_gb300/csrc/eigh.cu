@@ -804,15 +804,19 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
         col[r] = (r == 0) ? make_double2(1.0, 0.0) : A[(k + 1 + r) + (int64_t)k * n];
       __syncthreads();
       for (int jj = tid; jj < n; jj += VNT) {
-        double2 s0 = make_double2(0.0, 0.0), s1 = make_double2(0.0, 0.0);
+        double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
         int r = 0;
-        for (; r + 1 < m; r += 2) {
-          s0 = cfma_conj(col[r], Y[(int64_t)(k + 1 + r) * n + jj], s0);
-          s1 = cfma_conj(col[r + 1], Y[(int64_t)(k + 2 + r) * n + jj], s1);
+        for (; r + 3 < m; r += 4) {
+          const double2 y0 = Y[(int64_t)(k + 1 + r) * n + jj], y1 = Y[(int64_t)(k + 2 + r) * n + jj];
+          const double2 y2 = Y[(int64_t)(k + 3 + r) * n + jj], y3 = Y[(int64_t)(k + 4 + r) * n + jj];
+          s0 = cfma_conj(col[r], y0, s0);
+          s1 = cfma_conj(col[r + 1], y1, s1);
+          s2 = cfma_conj(col[r + 2], y2, s2);
+          s3 = cfma_conj(col[r + 3], y3, s3);
         }
-        if (r < m) s0 = cfma_conj(col[r], Y[(int64_t)(k + 1 + r) * n + jj], s0);
-        s0.x += s1.x;
-        s0.y += s1.y;
+        for (; r < m; ++r) s0 = cfma_conj(col[r], Y[(int64_t)(k + 1 + r) * n + jj], s0);
+        s0.x += s1.x + (s2.x + s3.x);
+        s0.y += s1.y + (s2.y + s3.y);
         const double2 ts = cmul(tau, s0);          // y -= tau v (v^H y)
         for (int q = 0; q < m; ++q) {
           double2 y = Y[(int64_t)(k + 1 + q) * n + jj];
@@ -830,14 +834,19 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
       __syncthreads();
       const double rl = 1.0 / col[max_n - 1].x;
       for (int jj = tid; jj < n; jj += VNT) {
-        double2 acc0 = Y[(int64_t)i * n + jj], acc1 = make_double2(0.0, 0.0);
+        double2 acc0 = Y[(int64_t)i * n + jj], acc1 = make_double2(0.0, 0.0), acc2 = acc1, acc3 = acc1;
         int r = 0;
-        for (; r + 1 < m; r += 2) {
-          acc0 = cfms_conj_l(col[r], Y[(int64_t)(i + 1 + r) * n + jj], acc0);
-          acc1 = cfms_conj_l(col[r + 1], Y[(int64_t)(i + 2 + r) * n + jj], acc1);
+        for (; r + 3 < m; r += 4) {
+          const double2 y0 = Y[(int64_t)(i + 1 + r) * n + jj], y1 = Y[(int64_t)(i + 2 + r) * n + jj];
+          const double2 y2 = Y[(int64_t)(i + 3 + r) * n + jj], y3 = Y[(int64_t)(i + 4 + r) * n + jj];
+          acc0 = cfms_conj_l(col[r], y0, acc0);
+          acc1 = cfms_conj_l(col[r + 1], y1, acc1);
+          acc2 = cfms_conj_l(col[r + 2], y2, acc2);
+          acc3 = cfms_conj_l(col[r + 3], y3, acc3);
         }
-        if (r < m) acc0 = cfms_conj_l(col[r], Y[(int64_t)(i + 1 + r) * n + jj], acc0);
-        Y[(int64_t)i * n + jj] = make_double2((acc0.x + acc1.x) * rl, (acc0.y + acc1.y) * rl);
+        for (; r < m; ++r) acc0 = cfms_conj_l(col[r], Y[(int64_t)(i + 1 + r) * n + jj], acc0);
+        Y[(int64_t)i * n + jj] = make_double2((acc0.x + acc1.x + (acc2.x + acc3.x)) * rl,
+                                              (acc0.y + acc1.y + (acc2.y + acc3.y)) * rl);
       }
       __syncthreads();
     }
@@ -907,17 +916,33 @@ extern "C" int SKN_EXPORT(skn_eigh_gen_batched_real)(int n_prob, const int32_t* 
   return launch_values<true>(n_prob, n, hs_off, eig_off, order, H, S, eig, status, work_counter, max_n, stream);
 }
 
-static int vec_grid(int n_prob) {
-  int dev = 0, sms = 0;
+// CTAs of the vector stage: as many as fit on the GPU at once (the stage is latency-bound, so
+// occupancy matters), but no more than the problems, and no more than keep the inverse-iteration
+// scratch (5 * max_n * VNT doubles per CTA) within VEC_SCRATCH_BUDGET.  Each problem is solved by
+// one CTA, so the results do not depend on the grid.
+constexpr int64_t VEC_SCRATCH_BUDGET = (int64_t)2 << 30;
+static int vec_grid(int n_prob, int max_n) {
+  int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int g = 2 * (sms > 0 ? sms : 1);
-  return g < n_prob ? g : (n_prob > 0 ? n_prob : 1);
+  if (sms < 1) sms = 1;
+  const int mn = max_n < 1 ? 1 : max_n;
+  if (set_smem_limit_once() != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eigvec, VNT, vec_smem_bytes(mn)) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 2;
+  int64_t g = (int64_t)sms * per_sm;
+  const int64_t per_cta = (int64_t)5 * mn * VNT * (int64_t)sizeof(double);
+  const int64_t cap = VEC_SCRATCH_BUDGET / per_cta;
+  if (g > cap) g = cap;
+  if (g < sms) g = sms < n_prob ? sms : n_prob;      // never fewer than one CTA per SM (or per problem)
+  if (g > n_prob) g = n_prob;
+  return g > 0 ? (int)g : 1;
 }
 
 extern "C" int SKN_EXPORT(skn_eigh_vectors_scratch_bytes)(int n_prob, int max_n, int64_t* bytes) {
   if (!bytes || max_n < 0 || n_prob < 0) return SKN_ERR_ARG;
-  *bytes = (int64_t)vec_grid(n_prob) * 5 * (int64_t)(max_n < 1 ? 1 : max_n) * VNT * (int64_t)sizeof(double);
+  *bytes = (int64_t)vec_grid(n_prob, max_n) * 5 * (int64_t)(max_n < 1 ? 1 : max_n) * VNT * (int64_t)sizeof(double);
   return SKN_OK;
 }
 
@@ -953,7 +978,7 @@ extern "C" int SKN_EXPORT(skn_eigh_gen_vectors)(int n_prob, const int32_t* n, co
   if (cudaPeekAtLastError() != cudaSuccess) return SKN_ERR_CUDA;
   const size_t vsmem = sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;
 
-  k_eigvec<<<vec_grid(n_prob), VNT, vsmem, stream>>>(n_prob, n, hs_off, eig_off, order, (const double2*)H,
+  k_eigvec<<<vec_grid(n_prob, mn), VNT, vsmem, stream>>>(n_prob, n, hs_off, eig_off, order, (const double2*)H,
                                                      (const double2*)S, eig, tri, status, (double2*)vec, scratch,
                                                      work_counter + 1, mn);
   return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;

@@ -11,6 +11,7 @@ sums -> eigensolve -> Fermi/gap -> DOS.
 """
 from __future__ import annotations
 
+import copy
 import ctypes
 import math
 import threading
@@ -130,6 +131,30 @@ class TableSet:
                 orb.extend([e[l]] * (2 * l + 1))
             self.sp_onsite.append(np.array(orb))
             self.sp_nelec[i] = float(np.sum(occupations[z]))
+
+    def with_values(self) -> Optional["TableSet"]:
+        """A TableSet with this one's layout and the current values of the tensors it was packed
+        from (one concatenation each for H and S), or None when some table was not a tensor.
+        This object is left unchanged, so engines still using it are unaffected."""
+        lists = self.__dict__.get("_value_lists")
+        if lists is None:
+            hs = [t for t, kind, _, _ in self.param_slices if kind == "H"]
+            ss = [t for t, kind, _, _ in self.param_slices if kind == "S"]
+            lists = (hs, ss)
+            self.__dict__["_value_lists"] = lists
+        hs, ss = lists
+        if len(hs) != self.ntab or len(ss) != self.ntab or self.ntab == 0:
+            return None
+        dev = self.device
+        if any(t.device != dev or t.dtype != torch.float64 for t in (hs[0], ss[0], hs[-1], ss[-1])):
+            flat = lambda t: t.detach().reshape(-1).to(dev, torch.float64)   # noqa: E731
+        else:
+            flat = lambda t: t.detach().view(-1)                             # noqa: E731
+        new = copy.copy(self)
+        with torch.no_grad():
+            new.tab_H = torch.cat([flat(t) for t in hs])
+            new.tab_S = torch.cat([flat(t) for t in ss])
+        return new
 
     @classmethod
     def from_synthetic(cls, tables: dict, shell_dict, device):

@@ -160,6 +160,27 @@ class SkfParameterOptimizer(nn.Module):
     def grid_step(self) -> float:
         return self.grid[1] - self.grid[0]
 
+    def constraint_bounds(self, c=(0.9, 0.7, 0.95, 0.9), device=None):
+        """(parameters, lower, upper) of ``apply_constraints``: the same bounds as tensors, so a
+        caller can clamp many pairs at once."""
+        ps, lo, hi = [], [], []
+        for key, p in self.h_params.items():
+            o = self.original_h_params[key].to(device if device is not None else p.device)
+            f = c[0] if key.split("-")[0] == key.split("-")[1] else c[1]
+            ps.append(p)
+            lo.append(o * f)
+            hi.append(o * (1 + (1 - f)))
+        for key, p in self.s_params.items():
+            o = self.original_s_params[key].to(device if device is not None else p.device)
+            ps.append(p)
+            if key.split("-")[0] == key.split("-")[1]:
+                lo.append(torch.maximum(o * c[2], torch.tensor(0.1, dtype=o.dtype, device=o.device)))
+                hi.append(o * (1 + (1 - c[2])))
+            else:
+                lo.append(o * c[3])
+                hi.append(o * (1 + (1 - c[3])))
+        return ps, lo, hi
+
     def apply_constraints(self, c=(0.9, 0.7, 0.95, 0.9)):
         """Clamp parameters to a band around their initial values (slakonet/optim.py:1392-1434)."""
         # same bounds as the reference, applied in place (which the table cache sees)
@@ -278,9 +299,29 @@ class MultiElementSkfParameterOptimizer(nn.Module):
             out[key] = d
         return out
 
-    def apply_constraints(self):
-        for opt in self.skf_optimizers.values():
-            opt.apply_constraints()
+    def apply_constraints(self, c=(0.9, 0.7, 0.95, 0.9)):
+        """Every pair's ``apply_constraints`` (slakonet/optim.py:1392-1434) at once: the bounds are
+        built on the parameters' device the first time and kept, and the clamp
+        min(max(p, lower), upper) -- exactly torch.clamp, including its behaviour when lower > upper
+        for negative amplitudes -- runs as two fused in-place operations over all parameters."""
+        plist = self._param_list()
+        key = (_PARAM_EPOCH[0], tuple(c), tuple(sorted({str(p.device) for p in plist})))
+        cached = self.__dict__.get("_bounds")
+        if cached is None or cached[0] != key:
+            ps, lo, hi = [], [], []
+            for opt in self.skf_optimizers.values():
+                a, b, d = opt.constraint_bounds(c)
+                ps += a
+                lo += b
+                hi += d
+            cached = (key, ps, lo, hi)
+            self.__dict__["_bounds"] = cached
+        _, ps, lo, hi = cached
+        if not ps:
+            return
+        with torch.no_grad():
+            torch._foreach_maximum_(ps, lo)
+            torch._foreach_minimum_(ps, hi)
 
     # ------------------------------------------------------------- feeding
     def __setattr__(self, name, value):
@@ -288,15 +329,20 @@ class MultiElementSkfParameterOptimizer(nn.Module):
         if name == "skf_optimizers":
             _bump_epoch()
 
-    def _param_signature(self, device):
+    def _param_list(self):
         cached = self.__dict__.get("_plist")
-        if cached is None or cached[0] != _PARAM_EPOCH[0] or cached[1] != self._invalidations:
+        if cached is None or cached[0] != _PARAM_EPOCH[0]:
             plist = [p for opt in self.skf_optimizers.values()
                      for p in itertools.chain(opt.h_params.values(), opt.s_params.values())]
-            cached = (_PARAM_EPOCH[0], self._invalidations, plist)
+            cached = (_PARAM_EPOCH[0], plist)
             self.__dict__["_plist"] = cached
-        # version counters only grow, so their sum changes whenever any of them does
-        return (str(device), cached[0], cached[1], sum(map(operator.attrgetter("_version"), cached[2])))
+        return cached[1]
+
+    def _param_signature(self, device):
+        """(layout key, value key): the layout changes with the parameter set, the value key with any
+        in-place update (version counters only grow, so their sum changes whenever any of them does)."""
+        plist = self._param_list()
+        return (str(device), _PARAM_EPOCH[0], self._invalidations), sum(map(operator.attrgetter("_version"), plist))
 
     def invalidate_tables(self):
         """Repack the device tables on the next call (needed only after assigning ``p.data`` directly)."""
@@ -305,10 +351,15 @@ class MultiElementSkfParameterOptimizer(nn.Module):
     def table_set(self, shell_dict: Dict[int, List[int]], device, species: Optional[Sequence[int]] = None):
         """Packed device tables for ``species`` (all elements of the model by default), cached."""
         species = sorted(set(int(z) for z in (species if species is not None else self._elements())))
-        key = (self._param_signature(device), tuple(species),
-               tuple((z, tuple(shell_dict[z])) for z in species))
+        layout, values = self._param_signature(device)
+        key = (layout, tuple(species), tuple((z, tuple(shell_dict[z])) for z in species))
         if self._table_cache is not None and self._table_cache[0] == key:
-            return self._table_cache[1]
+            if self._table_cache[2] == values:
+                return self._table_cache[1]
+            ts = self._table_cache[1].with_values()      # same layout, new values: repack values only
+            if ts is not None:
+                self._table_cache = (key, ts, values)
+                return ts
         h, s, steps, onsite, occ = {}, {}, {}, {}, {}
         sset = set(species)
         for key_, opt in self.skf_optimizers.items():
@@ -325,7 +376,7 @@ class MultiElementSkfParameterOptimizer(nn.Module):
         if missing:
             raise ValueError(f"no homonuclear parameters (on-site energies) for Z={missing}")
         ts = E.TableSet(species, shell_dict, h, s, steps, onsite, occ, device)
-        self._table_cache = (key, ts)
+        self._table_cache = (key, ts, values)
         return ts
 
     def _elements(self):

@@ -170,3 +170,24 @@ def test_device_tables_repack_exactly_when_parameters_change():
     assert model.table_set(sd, "cpu") is ts4
     model.invalidate_tables()                                      # ... until invalidated
     assert model.table_set(sd, "cpu") is not ts4
+
+
+def test_model_constraints_equal_the_per_pair_clamp():
+    """The fused model-level clamp gives exactly the per-pair loop's values (including negative amplitudes)."""
+    import copy
+    import torch
+    sd = {6: [0, 1], 14: [0, 1, 2]}
+    a = M.MultiElementSkfParameterOptimizer.from_tables(syn.make_tables([6, 14], sd, seed=2))
+    g = torch.Generator().manual_seed(0)
+    with torch.no_grad():
+        for p in a.parameters():
+            p.mul_(1.0 + 0.4 * torch.randn(p.shape, generator=g, dtype=p.dtype))
+    b = copy.deepcopy(a)
+    a.apply_constraints()
+    for opt in b.skf_optimizers.values():
+        opt.apply_constraints()
+    for (ka, pa), (kb, pb) in zip(a.named_parameters(), b.named_parameters()):
+        assert ka == kb and torch.equal(pa, pb), ka
+    a.apply_constraints()                      # idempotent
+    for (ka, pa), (kb, pb) in zip(a.named_parameters(), b.named_parameters()):
+        assert torch.equal(pa, pb), ka
