@@ -422,6 +422,57 @@ def run_large_structure(dev):
                     f"{E.cluster_for(n)} CTAs per k-point"}
 
 
+def run_reference_gpu(dev, sts, tables, sd, stride=32, limit=8):
+    """The plain per-structure GPU path: the reference package itself (installed in baseline/_ref by
+    ``pip install --target baseline/_ref <reference>``) with device="cuda", one structure per call, on
+    every ``stride``-th structure of the workload by size.  Its optional imports (ase, jarvis,
+    matplotlib, tqdm, requests, pydantic_settings) are stood in for, as in the golden-fixture harness;
+    the Gamma-centred k-points are injected the same way.  Returns None when baseline/_ref is absent."""
+    import types
+    import torch
+    ref_root = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref_root, "slakonet")):
+        return None
+    for name in ("tqdm", "requests", "pydantic_settings"):
+        try:
+            __import__(name)
+        except ImportError:
+            m = types.ModuleType(name)
+            m.tqdm = lambda it=None, *a, **k: it
+            m.BaseSettings = object
+            m.SettingsConfigDict = dict
+            sys.modules[name] = m
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import refharness
+    refharness.REF_ROOT = ref_root
+    ref = refharness.import_reference()
+    model = refharness.build_reference_model(ref, tables)
+    sample = cpu_sample(sts, stride)[:limit]
+    P = ref.atoms.Periodic
+    orig = P._kpoints
+    tot_k, tot_t, per = 0, 0.0, []
+    for st in sample:
+        k = torch.tensor(np.asarray(st["kpoints"], dtype=np.float64))
+        P._kpoints = lambda this, _k=k, **kw: (_k.unsqueeze(0), torch.tensor([len(_k)]),
+                                                torch.full((1, len(_k)), 1.0 / len(_k)))
+        geom = ref.atoms.Geometry(torch.tensor(st["numbers"]).unsqueeze(0),
+                                  torch.tensor(st["positions"]).unsqueeze(0), cell=torch.tensor(st["cell"]).unsqueeze(0))
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        with torch.no_grad():
+            model.compute_multi_element_properties(geometry=geom, shell_dict=sd, device=str(dev), get_fermi=True)
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t
+        P._kpoints = orig
+        per.append({"atoms": len(st["numbers"]), "n": orbitals(st, sd), "k_points": len(k), "seconds": round(dt, 3)})
+        tot_k += len(k)
+        tot_t += dt
+    return {"value": tot_k / tot_t, "unit": UNIT, "structures": len(sample), "k_point_solves": tot_k,
+            "seconds": tot_t, "per_structure": per,
+            "sample": f"every {stride}th structure by size, first {limit}; the reference's "
+                      "compute_multi_element_properties(device='cuda', get_fermi=True), one structure per call"}
+
+
 def run_cpu_baseline(sts, tables, sd, reps=1):
     _single_thread_workers()
     sample = cpu_sample(sts)
@@ -479,6 +530,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the training-step and serving measurements")
     ap.add_argument("--serving-requests", type=int, default=200, help="requests in the serving stream")
     ap.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream (1/s)")
+    ap.add_argument("--reference-gpu", action="store_true",
+                    help="also time the reference package (baseline/_ref) per structure on the GPU, on a sample")
     ap.add_argument("--large-structure", action="store_true",
                     help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
     args = ap.parse_args()
@@ -501,6 +554,10 @@ def main():
             out["training_step"] = run_training_step(dev)
             log("serving")
             out["serving"] = run_serving(dev, args.serving_requests, args.serving_rate)
+        if world == 1 and args.reference_gpu:
+            import torch
+            log("reference per-structure GPU path")
+            out["reference_gpu_path"] = run_reference_gpu(torch.device("cuda", 0), sts, tables, sd)
         if world == 1 and args.large_structure:
             import torch
             log("large structure")

@@ -1,10 +1,12 @@
 """Import harness for the reference SlakoNet package (fixture generation only).
 
 This module is used by ``make_golden.py`` in a container that holds a
-read-only copy of the reference at ``/root/reference``.  It is never
-imported by the library, by ``bench.py`` or by the GPU tests: the reference
-does not exist on the GPU hosts.  The committed golden fixtures are what
-travels.
+read-only copy of the reference at ``/root/reference``.  The library and the
+GPU tests never import it: the reference source tree does not exist on the
+GPU hosts, and the committed golden fixtures are what travels.  The one other
+user is ``bench.py --reference-gpu``, which points ``REF_ROOT`` at a pip
+installation of the reference in ``baseline/_ref`` (when present) to time the
+reference's own per-structure GPU path.
 
 The reference imports ``ase``, ``jarvis`` and ``matplotlib`` at module level
 (slakonet/main.py:4-20, slakonet/optim.py:19-36).  None of them is on the
