@@ -442,6 +442,9 @@ def run_reference_gpu(dev, sts, tables, sd, stride=32, limit=8):
             m.BaseSettings = object
             m.SettingsConfigDict = dict
             sys.modules[name] = m
+    # the reference turns on torch.use_deterministic_algorithms when imported
+    # (slakonet/optim.py:55-59), under which torch refuses cuBLAS calls unless this is set
+    os.environ.setdefault("CUBLAS_WORKSPACE_CONFIG", ":4096:8")
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
     import refharness
     refharness.REF_ROOT = ref_root
@@ -471,6 +474,50 @@ def run_reference_gpu(dev, sts, tables, sd, stride=32, limit=8):
             "seconds": tot_t, "per_structure": per,
             "sample": f"every {stride}th structure by size, first {limit}; the reference's "
                       "compute_multi_element_properties(device='cuda', get_fermi=True), one structure per call"}
+
+
+def run_reference_gpu_training(dev, n=3):
+    """The reference's own training forward + backward (autograd through its eighb, Bloch sums and
+    splines) on the GPU for the first ``n`` structures of the config-3 fitting batch, one structure per
+    call as its fitting loop runs them (slakonet/optim.py:1656-1772), loss = DOS MSE + |gap| against
+    zero targets (the cost does not depend on the targets).  Needs baseline/_ref (see run_reference_gpu)."""
+    import torch
+    from slakonet_gb300 import synthetic as syn, training as T
+    ref_root = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref_root, "slakonet")):
+        return None
+    import refharness                    # made importable by run_reference_gpu
+    ref = refharness.import_reference()
+    sts = T.fitting_batch(64, seed=SEED)
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    sd = syn.default_shell_dict()
+    model = refharness.build_reference_model(ref, syn.make_tables(zs, sd, seed=SEED))
+    P = ref.atoms.Periodic
+    orig = P._kpoints
+    per, losses = [], []
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for st in sts[:n]:
+        k = torch.tensor(np.asarray(st["kpoints"], dtype=np.float64))
+        P._kpoints = lambda this, _k=k, **kw: (_k.unsqueeze(0), torch.tensor([len(_k)]),
+                                                torch.full((1, len(_k)), 1.0 / len(_k)))
+        geom = ref.atoms.Geometry(torch.tensor(st["numbers"]).unsqueeze(0),
+                                  torch.tensor(st["positions"]).unsqueeze(0), cell=torch.tensor(st["cell"]).unsqueeze(0))
+        t = time.perf_counter()
+        props, ok = model.compute_multi_element_properties(geometry=geom, shell_dict=sd, device=str(dev))
+        dos = props["dos_values_tensor"]
+        losses.append(torch.mean(dos ** 2) + torch.abs(props["band_gap_eV"]))
+        torch.cuda.synchronize(dev)
+        per.append({"atoms": len(st["numbers"]), "k_points": len(k), "forward_s": round(time.perf_counter() - t, 3)})
+        P._kpoints = orig
+    t = time.perf_counter()
+    torch.stack([x.reshape(()) for x in losses]).sum().backward()
+    torch.cuda.synchronize(dev)
+    back = time.perf_counter() - t
+    total = time.perf_counter() - t0
+    return {"structures": n, "seconds": total, "backward_s": back, "per_structure": per,
+            "seconds_per_structure": total / n, "projected_64_structure_step_s": total / n * 64,
+            "note": "reference package on the GPU, autograd; projected step = 64 x the per-structure time"}
 
 
 def run_cpu_baseline(sts, tables, sd, reps=1):
@@ -554,14 +601,25 @@ def main():
             out["training_step"] = run_training_step(dev)
             log("serving")
             out["serving"] = run_serving(dev, args.serving_requests, args.serving_rate)
-        if world == 1 and args.reference_gpu:
-            import torch
-            log("reference per-structure GPU path")
-            out["reference_gpu_path"] = run_reference_gpu(torch.device("cuda", 0), sts, tables, sd)
         if world == 1 and args.large_structure:
             import torch
             log("large structure")
             out["large_structure"] = run_large_structure(torch.device("cuda", 0))
+        if world == 1 and args.reference_gpu:      # last: importing the reference changes torch's global state
+            import torch
+            state = (torch.are_deterministic_algorithms_enabled(), torch.get_default_dtype(),
+                     torch.backends.cudnn.deterministic, torch.backends.cudnn.benchmark)
+            import contextlib
+            try:
+                with contextlib.redirect_stdout(sys.stderr):      # the reference prints progress
+                    log("reference per-structure GPU path")
+                    out["reference_gpu_path"] = run_reference_gpu(torch.device("cuda", 0), sts, tables, sd)
+                    log("reference training step on the GPU")
+                    out["reference_gpu_training"] = run_reference_gpu_training(torch.device("cuda", 0))
+            finally:
+                torch.use_deterministic_algorithms(state[0])
+                torch.set_default_dtype(state[1])
+                torch.backends.cudnn.deterministic, torch.backends.cudnn.benchmark = state[2], state[3]
         if world == 1 and not args.no_cpu_baseline:
             log("cpu baseline")
             out["cpu_baseline"] = run_cpu_baseline(sts, tables, sd)
