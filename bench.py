@@ -520,6 +520,32 @@ def run_reference_gpu_training(dev, n=3):
             "note": "reference package on the GPU, autograd; projected step = 64 x the per-structure time"}
 
 
+def run_reference_gpu_subprocess(args) -> dict:
+    """Both reference measurements in a fresh process: importing the reference turns on torch's
+    deterministic mode (slakonet/optim.py:55-59), which needs CUBLAS_WORKSPACE_CONFIG set before the
+    process first uses cuBLAS, and changes torch's default dtype."""
+    env = dict(os.environ, CUBLAS_WORKSPACE_CONFIG=":4096:8")
+    cmd = [sys.executable, os.path.abspath(__file__), "--reference-gpu-worker", "--structures", str(args.structures),
+           "--seed", str(args.seed)]
+    r = subprocess.run(cmd, env=env, capture_output=True, text=True)
+    sys.stderr.write(r.stderr[-2000:])
+    try:
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    except (ValueError, IndexError):
+        return {"reference_gpu_path": {"unavailable": f"worker exited {r.returncode}"}}
+
+
+def reference_gpu_worker(args):
+    import contextlib
+    import torch
+    sts, tables, sd = workload(args.structures, args.seed)
+    dev = torch.device("cuda", 0)
+    with contextlib.redirect_stdout(sys.stderr):      # the reference prints progress
+        a = run_reference_gpu(dev, sts, tables, sd)
+        b = run_reference_gpu_training(dev)
+    print(json.dumps({"reference_gpu_path": a, "reference_gpu_training": b}))
+
+
 def run_cpu_baseline(sts, tables, sd, reps=1):
     _single_thread_workers()
     sample = cpu_sample(sts)
@@ -579,11 +605,15 @@ def main():
     ap.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream (1/s)")
     ap.add_argument("--reference-gpu", action="store_true",
                     help="also time the reference package (baseline/_ref) per structure on the GPU, on a sample")
+    ap.add_argument("--reference-gpu-worker", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--large-structure", action="store_true",
                     help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.reference_gpu_worker:
+        reference_gpu_worker(args)
+        return
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)))
@@ -605,21 +635,9 @@ def main():
             import torch
             log("large structure")
             out["large_structure"] = run_large_structure(torch.device("cuda", 0))
-        if world == 1 and args.reference_gpu:      # last: importing the reference changes torch's global state
-            import torch
-            state = (torch.are_deterministic_algorithms_enabled(), torch.get_default_dtype(),
-                     torch.backends.cudnn.deterministic, torch.backends.cudnn.benchmark)
-            import contextlib
-            try:
-                with contextlib.redirect_stdout(sys.stderr):      # the reference prints progress
-                    log("reference per-structure GPU path")
-                    out["reference_gpu_path"] = run_reference_gpu(torch.device("cuda", 0), sts, tables, sd)
-                    log("reference training step on the GPU")
-                    out["reference_gpu_training"] = run_reference_gpu_training(torch.device("cuda", 0))
-            finally:
-                torch.use_deterministic_algorithms(state[0])
-                torch.set_default_dtype(state[1])
-                torch.backends.cudnn.deterministic, torch.backends.cudnn.benchmark = state[2], state[3]
+        if world == 1 and args.reference_gpu:
+            log("reference per-structure GPU path and training step (subprocess)")
+            out.update(run_reference_gpu_subprocess(args))
         if world == 1 and not args.no_cpu_baseline:
             log("cpu baseline")
             out["cpu_baseline"] = run_cpu_baseline(sts, tables, sd)
