@@ -227,59 +227,73 @@ class Plan:
 
 def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUTOFF_BOHR) -> Plan:
     """Flat descriptors for a batch.  Each structure: numbers, positions (Bohr),
-    cell (Bohr, rows = lattice vectors), kpoints [nk,3] fractional, optional weights."""
+    cell (Bohr, rows = lattice vectors), kpoints [nk,3] fractional, optional weights.
+
+    The per-structure loop only gathers arrays and sizes the translation box;
+    everything per atom or per orbital is built with whole-batch array operations."""
     S = len(structures)
-    atom_ptr = np.zeros(S + 1, np.int32)
-    orb_ptr = np.zeros(S + 1, np.int32)
-    k_ptr = np.zeros(S + 1, np.int32)
-    pos, cells, rng, species, norb, aoff, oatom, onsite = [], [], [], [], [], [], [], []
-    kp, kw, nums, nelec = [], [], [], np.zeros(S)
-    pair_base = np.zeros(S, np.int64)
-    phase_base = np.zeros(S, np.int64)
+    nums, pos, cells, kp, kw = [], [], [], [], []
+    n_at = np.zeros(S, np.int64)
     nk = np.zeros(S, np.int32)
-    nb = np.zeros(S, np.int32)
-    pb = 0
-    phb = 0
-    ninj = []
+    rng = np.zeros((S, 3), np.int32)
     for s, st in enumerate(structures):
         z = np.asarray(st["numbers"], dtype=np.int64).reshape(-1)
         p = np.asarray(st["positions"], dtype=np.float64).reshape(-1, 3)
         c = np.asarray(st["cell"], dtype=np.float64).reshape(3, 3)
         k = np.asarray(st["kpoints"], dtype=np.float64).reshape(-1, 3)
         w = np.asarray(st.get("weights", np.full(len(k), 1.0 / max(len(k), 1))), dtype=np.float64)
-        try:
-            sp = np.array([tables.sp_of[int(a)] for a in z], np.int32)
-        except KeyError as e:
-            raise ValueError(f"no parameters for element Z={e.args[0]}") from None
-        no = tables.sp_norb_np[sp]
-        N = len(z)
-        atom_ptr[s + 1] = atom_ptr[s] + N
-        orb_ptr[s + 1] = orb_ptr[s] + int(no.sum())
-        k_ptr[s + 1] = k_ptr[s] + len(k)
+        nums.append(z)
         pos.append(p)
         cells.append(c)
-        r = image_range(c, p, cutoff)
-        rng.append(r)
-        species.append(sp)
-        norb.append(no)
-        off = np.concatenate([[0], np.cumsum(no)[:-1]]).astype(np.int32)
-        aoff.append(off)
-        oatom.append(np.repeat(np.arange(N, dtype=np.int32), no))
-        onsite.append(np.concatenate([tables.sp_onsite[q] for q in sp]))
         kp.append(k)
         kw.append(w)
-        nums.append(z)
-        nelec[s] = float(tables.sp_nelec[sp].sum())
-        pair_base[s] = pb
-        pb += N * N
-        ninj.append(np.outer(no, no).reshape(-1))
-        nimg = int(np.prod(2 * r + 1))
-        phase_base[s] = phb
-        phb += nimg * len(k)
+        n_at[s] = len(z)
         nk[s] = len(k)
-        nb[s] = int(no.sum())
+        rng[s] = image_range(c, p, cutoff)
+    zall = np.concatenate(nums) if S else np.zeros(0, np.int64)
+    lut = tables.__dict__.get("_species_lut")
+    if lut is None:
+        lut = np.full(max(tables.species) + 1, -1, np.int32)
+        for z_, i in tables.sp_of.items():
+            lut[z_] = i
+        tables.__dict__["_species_lut"] = lut
+    bad = (zall < 0) | (zall >= len(lut))
+    species = np.where(bad, -1, lut[np.clip(zall, 0, len(lut) - 1)]).astype(np.int32)
+    if (species < 0).any():
+        raise ValueError(f"no parameters for element Z={int(zall[np.argmax(species < 0)])}")
+    norb = tables.sp_norb_np[species].astype(np.int32)
+    atom_ptr = np.zeros(S + 1, np.int32)
+    atom_ptr[1:] = np.cumsum(n_at)
+    atom_struct = np.repeat(np.arange(S), n_at)
+    orb_cum = np.concatenate([[0], np.cumsum(norb, dtype=np.int64)])
+    orb_ptr = orb_cum[atom_ptr].astype(np.int32)
+    nb = np.diff(orb_ptr).astype(np.int32)
+    aoff = (orb_cum[:-1] - orb_ptr[atom_struct]).astype(np.int32)            # first local orbital per atom
+    oatom = np.repeat(np.arange(len(zall)) - atom_ptr[atom_struct], norb).astype(np.int32)
+    ons = tables.__dict__.get("_species_onsite_flat")
+    if ons is None:
+        ons = (np.concatenate([[0], np.cumsum([len(v) for v in tables.sp_onsite])]).astype(np.int64),
+               np.concatenate(tables.sp_onsite) if tables.sp_onsite else np.zeros(0))
+        tables.__dict__["_species_onsite_flat"] = ons
+    first = np.repeat(ons[0][species], norb)                                   # per orbital: start of its species
+    within = np.arange(int(orb_cum[-1])) - np.repeat(orb_cum[:-1], norb)       # orbital index within its atom
+    onsite = ons[1][first + within] if len(first) else np.zeros(0)
+    nelec = np.add.reduceat(tables.sp_nelec[species], atom_ptr[:-1]) if len(zall) else np.zeros(S)
+    nelec = np.where(n_at > 0, nelec, 0.0).astype(np.float64)
+    pair_sz = n_at * n_at
+    pair_base = np.concatenate([[0], np.cumsum(pair_sz)[:-1]]).astype(np.int64)
+    pb = int(pair_sz.sum())
+    # norb_i * norb_j for every ordered atom pair, structure by structure
+    ninj = np.concatenate([np.outer(norb[atom_ptr[s]:atom_ptr[s + 1]], norb[atom_ptr[s]:atom_ptr[s + 1]]).reshape(-1)
+                           for s in range(S)]).astype(np.int64) if S else np.zeros(0, np.int64)
+    k_ptr = np.zeros(S + 1, np.int32)
+    k_ptr[1:] = np.cumsum(nk)
+    nimg = np.prod(2 * rng.astype(np.int64) + 1, axis=1)
+    ph_sz = nimg * nk
+    phase_base = np.concatenate([[0], np.cumsum(ph_sz)[:-1]]).astype(np.int64)
+    phb = int(ph_sz.sum())
     prob_struct = np.repeat(np.arange(S, dtype=np.int32), nk)
-    prob_k = np.concatenate([np.arange(n, dtype=np.int32) for n in nk]) if S else np.zeros(0, np.int32)
+    prob_k = (np.arange(int(nk.sum()), dtype=np.int64) - np.repeat(k_ptr[:-1], nk)).astype(np.int32)
     prob_n = nb[prob_struct]
     sz = prob_n.astype(np.int64) ** 2
     hs_off = np.concatenate([[0], np.cumsum(sz)[:-1]]).astype(np.int64)
@@ -290,11 +304,10 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
     kw_off = k_ptr[:-1].astype(np.int64)
     kall = np.concatenate(kp) if S else np.zeros((0, 3))
     prob_real = np.all(2.0 * kall == np.round(2.0 * kall), axis=1)
-    return Plan(S, nums, atom_ptr, orb_ptr, np.concatenate(pos), np.stack(cells), np.stack(rng),
-                np.concatenate(species), np.concatenate(norb).astype(np.int32), np.concatenate(aoff),
-                np.concatenate(oatom), np.concatenate(onsite), pair_base, int(pb),
-                np.concatenate(ninj).astype(np.int64), k_ptr, np.concatenate(kp), np.concatenate(kw), kw_off,
-                nk, nb, phase_base, int(phb), prob_struct, prob_k, prob_n, hs_off, int(sz.sum()),
+    return Plan(S, nums, atom_ptr, orb_ptr, np.concatenate(pos) if S else np.zeros((0, 3)),
+                np.stack(cells) if S else np.zeros((0, 3, 3)), rng, species, norb, aoff, oatom, onsite,
+                pair_base, pb, ninj, k_ptr, kall, np.concatenate(kw) if S else np.zeros(0), kw_off,
+                nk, nb, phase_base, phb, prob_struct, prob_k, prob_n, hs_off, int(sz.sum()),
                 eig_off_prob, eig_off_struct, int(eig_sz.sum()), order, nelec, int(nb.max()) if S else 0,
                 prob_real=prob_real)
 
