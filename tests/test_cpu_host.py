@@ -191,3 +191,31 @@ def test_model_constraints_equal_the_per_pair_clamp():
     a.apply_constraints()                      # idempotent
     for (ka, pa), (kb, pb) in zip(a.named_parameters(), b.named_parameters()):
         assert torch.equal(pa, pb), ka
+
+
+def test_plan_batch_matches_per_structure_construction():
+    """The whole-batch descriptor construction equals building each structure's arrays on its own."""
+    sts = syn.uneven_batch(30, nmin=1, nmax=20, zmax=65, seed=21, kdens=200.0)
+    sd = syn.default_shell_dict()
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    ts = E.TableSet.from_synthetic(syn.make_tables(zs, sd, seed=21), {z: sd[z] for z in zs}, "cpu")
+    plan = E.plan_batch(sts, ts)
+    a0 = o0 = 0
+    for s, st in enumerate(sts):
+        z = np.asarray(st["numbers"])
+        sp = np.array([ts.sp_of[int(x)] for x in z])
+        no = ts.sp_norb_np[sp]
+        N = len(z)
+        assert plan.atom_ptr[s] == a0 and plan.orb_ptr[s] == o0
+        assert np.array_equal(plan.atom_species[a0:a0 + N], sp) and np.array_equal(plan.atom_norb[a0:a0 + N], no)
+        assert np.array_equal(plan.atom_orb_off[a0:a0 + N], np.concatenate([[0], np.cumsum(no)[:-1]]))
+        n = int(no.sum())
+        assert np.array_equal(plan.orb_atom[o0:o0 + n], np.repeat(np.arange(N), no))
+        assert np.array_equal(plan.onsite_H[o0:o0 + n], np.concatenate([ts.sp_onsite[q] for q in sp]))
+        assert plan.nelec[s] == float(ts.sp_nelec[sp].sum())
+        pb = int(plan.pair_base[s])
+        assert np.array_equal(plan.pair_ni_nj[pb:pb + N * N], np.outer(no, no).reshape(-1))
+        assert np.array_equal(plan.image_range[s], E.image_range(st["cell"], st["positions"], E.CUTOFF_BOHR))
+        a0 += N
+        o0 += n
+    assert plan.atom_ptr[-1] == a0 and plan.orb_ptr[-1] == o0
