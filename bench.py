@@ -347,15 +347,28 @@ def run_training_step(dev, steps=3):
             "note": "forward includes eigenvectors; gradient from the hand-written adjoint (csrc/adjoint.cu)"}
 
 
-def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40, capacity=True):
-    """Config-4 shape: Poisson stream of ``n_requests`` at ``rate`` per second, structures of 1-200 atoms
-    (log-uniform), Z 1-65, ~1000 k-atoms each; then the same requests submitted at once (capacity);
-    then a one-request-at-a-time baseline through the same API."""
+def serving_set(n_requests, path=None):
+    """The serving request set (``synthetic.serving_requests``), read from ``path`` when that file
+    exists, else generated on the host cores (and written to ``path`` when one is given)."""
+    from slakonet_gb300 import synthetic as syn
+    if path and os.path.exists(path):
+        sts = syn.load_structures(path)
+        if len(sts) != n_requests:
+            raise SystemExit(f"{path} holds {len(sts)} requests, not {n_requests}")
+        return sts, path
+    sts = syn.serving_requests(n_requests, processes=min(16, os.cpu_count() or 1))
+    if path:
+        syn.save_structures(path, sts)
+    return sts, "generated"
+
+
+def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40, capacity=True, path=None):
+    """Serving stream: ``n_requests`` Poisson arrivals at ``rate`` per second, structures of 1-200
+    atoms (log-uniform), Z 1-65, ~1000 k-atoms each; then the same requests submitted at once
+    (capacity); then a one-request-at-a-time baseline through the same API on ``seq_sample`` of them."""
     import torch
     from slakonet_gb300 import model as M, serving as SV, synthetic as syn
-    sts = syn.uneven_batch(n_requests, nmin=1, nmax=200, zmax=65, seed=SEED + 7)
-    for st in sts:
-        st["weights"] = np.full(len(st["kpoints"]), 1.0 / len(st["kpoints"]))
+    sts, source = serving_set(n_requests, path)
     sd = syn.default_shell_dict()
     zs = list(range(1, 66))
     tables = syn.make_tables(zs, sd, seed=SEED)
@@ -385,8 +398,10 @@ def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40, capacity=True):
                 "structures_per_s": len(lat_b) / wall_b, "k_point_solves_per_s": sum(nk) / wall_b,
                 "note": "the same requests submitted at once"},
             "sequential_baseline": None if not seq else {
-                "sample": seq_sample, "p50_ms": 1e3 * float(np.median(seq)), "structures_per_s": seq_sample / sum(seq)},
+                "sample": len(seq), "p50_ms": 1e3 * float(np.median(seq)), "structures_per_s": len(seq) / sum(seq)},
             "p90_ms": 1e3 * float(np.percentile(lat, 90)), "p999_ms": 1e3 * float(np.percentile(lat, 99.9)),
+            "max_ms": 1e3 * float(lat.max()), "wall_s": wall, "atoms_total": int(sum(len(st["numbers"]) for st in sts)),
+            "k_points_total": int(sum(nk)), "request_set": source,
             "workload": "Poisson arrivals; structures 1-200 atoms log-uniform, Z=1-65, Gamma-centred ~1000 k-atoms; "
                         "each response: eigenvalues, DOS, gap, Fermi level"}
 
@@ -606,6 +621,13 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the training-step and serving measurements")
     ap.add_argument("--serving-requests", type=int, default=200, help="requests in the serving stream")
     ap.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream (1/s)")
+    ap.add_argument("--serving-file", default=None,
+                    help="request-set file: read when it exists, else generated once and written there")
+    ap.add_argument("--serving-sequential", type=int, default=40,
+                    help="requests timed one at a time for the sequential baseline (0 skips it)")
+    ap.add_argument("--no-serving-capacity", action="store_true", help="skip the all-at-once capacity leg")
+    ap.add_argument("--serving-only", action="store_true",
+                    help="run only the serving measurement (one GPU) and print its JSON line with clocks")
     ap.add_argument("--reference-gpu", action="store_true",
                     help="also time the reference package (baseline/_ref) per structure on the GPU, on a sample")
     ap.add_argument("--reference-gpu-worker", action="store_true", help=argparse.SUPPRESS)
@@ -621,6 +643,15 @@ def main():
         if rank == 0:
             print(json.dumps(run_reference(args)))
         return
+    if args.serving_only:
+        import torch
+        dev = torch.device("cuda", 0)
+        with ClockSampler(0) as clk:
+            out = run_serving(dev, args.serving_requests, args.serving_rate, args.serving_sequential,
+                              not args.no_serving_capacity, args.serving_file)
+        out["clocks"] = clk.summary()
+        print(json.dumps(out))
+        return
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
@@ -633,7 +664,8 @@ def main():
             log("training step")
             out["training_step"] = run_training_step(dev)
             log("serving")
-            out["serving"] = run_serving(dev, args.serving_requests, args.serving_rate)
+            out["serving"] = run_serving(dev, args.serving_requests, args.serving_rate, args.serving_sequential,
+                                         not args.no_serving_capacity, args.serving_file)
         if world == 1 and args.large_structure:
             import torch
             log("large structure")

@@ -270,3 +270,62 @@ def uneven_batch(n_structures: int = 256, nmin: int = 2, nmax: int = 64, zmax: i
         st["kpoints"] = gamma_centred_kpoints(st["mesh"])
         out.append(st)
     return out
+
+
+# ------------------------------------------------------------ serving stream
+
+SERVING_CHUNK = 625        # structures per seeded chunk of the serving request set
+SERVING_SEED = 1000        # chunk i is drawn from seed SERVING_SEED + i
+SERVING_SHUFFLE_SEED = 5   # one permutation interleaves the chunks
+
+
+def _serving_chunk(args) -> List[dict]:
+    n, seed = args
+    return uneven_batch(n, nmin=1, nmax=200, zmax=65, seed=seed)
+
+
+def serving_requests(n_requests: int, processes: int = 1, chunk: int = SERVING_CHUNK, seed: int = SERVING_SEED,
+                     shuffle_seed: int = SERVING_SHUFFLE_SEED) -> List[dict]:
+    """Serving request set: structures of 1-200 atoms (log-uniform), Z 1-65, random triclinic
+    cells, Gamma-centred grids of ~1000 k-atoms, uniform k-point weights.
+
+    The set is drawn in chunks of ``chunk`` structures, chunk i from ``uneven_batch`` with seed
+    ``seed + i``, then shuffled by one seeded permutation.  The result depends only on the
+    arguments, not on ``processes`` (worker processes for the chunks, started with ``spawn`` so
+    that they are safe after CUDA is initialised)."""
+    jobs = [(min(chunk, n_requests - a), seed + i) for i, a in enumerate(range(0, n_requests, chunk))]
+    if processes > 1 and len(jobs) > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(processes, len(jobs))) as pool:
+            parts = pool.map(_serving_chunk, jobs)
+    else:
+        parts = [_serving_chunk(j) for j in jobs]
+    sts = [s for p in parts for s in p]
+    sts = [sts[i] for i in np.random.default_rng(shuffle_seed).permutation(len(sts))]
+    for st in sts:
+        st["weights"] = np.full(len(st["kpoints"]), 1.0 / len(st["kpoints"]))
+    return sts
+
+
+def save_structures(path: str, structures: List[dict]) -> None:
+    """Write structures (numbers, positions, cell, kpoints) to one compressed .npz."""
+    np.savez_compressed(path, natoms=np.array([len(s["numbers"]) for s in structures]),
+                        nk=np.array([len(s["kpoints"]) for s in structures]),
+                        numbers=np.concatenate([np.asarray(s["numbers"]) for s in structures]),
+                        positions=np.concatenate([np.asarray(s["positions"]) for s in structures]),
+                        cells=np.stack([np.asarray(s["cell"]) for s in structures]),
+                        kpoints=np.concatenate([np.asarray(s["kpoints"]) for s in structures]))
+
+
+def load_structures(path: str) -> List[dict]:
+    """Read a file written by ``save_structures``; k-point weights are uniform."""
+    with np.load(path) as z:
+        arr = {k: z[k] for k in z.files}      # each z[k] decompresses the whole array: read once
+    out, a, k = [], 0, 0
+    for i, (na, nk) in enumerate(zip(arr["natoms"].tolist(), arr["nk"].tolist())):
+        out.append({"numbers": arr["numbers"][a:a + na].copy(), "positions": arr["positions"][a:a + na].copy(),
+                    "cell": arr["cells"][i].copy(), "kpoints": arr["kpoints"][k:k + nk].copy(),
+                    "weights": np.full(nk, 1.0 / nk)})
+        a += na
+        k += nk
+    return out

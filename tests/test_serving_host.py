@@ -3,6 +3,7 @@ import threading
 import time
 
 import numpy as np
+import pytest
 
 from slakonet_gb300 import serving as SV, synthetic as syn
 
@@ -77,3 +78,43 @@ def test_batches_form_from_requests_that_arrive_during_execution():
     server.close()
     # the first batch holds one request; the rest arrived while it ran and were batched together
     assert sizes[0] == 1 and max(sizes[1:]) > 1
+
+
+_KEYS = ("numbers", "positions", "cell", "kpoints", "weights")
+
+
+def _same(a, b):
+    return len(a) == len(b) and all(np.array_equal(x[k], y[k]) for x, y in zip(a, b) for k in _KEYS)
+
+
+def test_serving_request_set_is_chunked_seeded_and_independent_of_processes():
+    serial = syn.serving_requests(5, chunk=2)
+    parallel = syn.serving_requests(5, chunk=2, processes=2)
+    assert _same(serial, parallel)
+    # chunk i is uneven_batch(seed = 1000 + i); one seeded permutation interleaves the chunks
+    chunks = (syn.uneven_batch(2, nmin=1, nmax=200, zmax=65, seed=1000)
+              + syn.uneven_batch(2, nmin=1, nmax=200, zmax=65, seed=1001)
+              + syn.uneven_batch(1, nmin=1, nmax=200, zmax=65, seed=1002))
+    order = np.random.default_rng(5).permutation(5)
+    for st, i in zip(serial, order):
+        for k in ("numbers", "positions", "cell", "kpoints"):
+            assert np.array_equal(st[k], chunks[i][k])
+        assert np.allclose(st["weights"].sum(), 1.0) and len(st["weights"]) == len(st["kpoints"])
+        assert 1 <= len(st["numbers"]) <= 200
+
+
+def test_serving_request_file_round_trip_and_bench_loader(tmp_path):
+    import importlib.util
+    import os
+    sts = syn.serving_requests(3, chunk=625)
+    path = str(tmp_path / "requests.npz")
+    syn.save_structures(path, sts)
+    assert _same(sts, syn.load_structures(path))
+    spec = importlib.util.spec_from_file_location(
+        "bench_for_test", os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    got, source = bench.serving_set(3, path)
+    assert source == path and _same(sts, got)
+    with pytest.raises(SystemExit):
+        bench.serving_set(4, path)
