@@ -3,7 +3,7 @@
 THIS MODULE IS TEST INFRASTRUCTURE.  It is a numpy restatement of the
 reference's algorithm and is imported only by ``tests/``, by
 ``__graft_entry__.smoke()`` and by ``bench.py`` (its CPU-baseline leg and the
-``--impl reference`` arm), always as the checker or the timed CPU baseline,
+``--impl reference`` arm), always as the parity reference or the timed CPU baseline,
 never as part of the product path.  The product path (``slakonet_gb300``)
 runs the CUDA kernels and fails loudly without them.
 
