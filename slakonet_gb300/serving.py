@@ -112,7 +112,8 @@ class Server:
             req = Request(self.rid, structure, n_orb, nk, request_bytes(n_orb, nk, self.dos["dos_points"]),
                           time.perf_counter())
         if n_orb > MAX_N:
-            self.rejected += 1
+            with self.cv:
+                self.rejected += 1
             req.future.set_exception(ValueError(f"{n_orb} orbitals exceed the eigensolver's {MAX_N}"))
             return req.future
         self.pending.put(req)
@@ -198,7 +199,8 @@ class Server:
             except Exception as e:   # surfaced on every request of the batch
                 outs, err = None, e
             t1 = time.perf_counter()
-            self.batches += 1
+            with self.cv:
+                self.batches += 1
             for i, r in enumerate(batch):
                 r.t_done = t1
                 self.adm.release(r.nbytes)
