@@ -191,6 +191,21 @@ def fp64_peak(torch, lib, dev):
     return best
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest ``x`` over all ranks: a job of replicas takes as long as its slowest rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, units_per_rank: int, steps: int, seconds: float) -> float:
+    """Whole-job throughput: every rank processes ``units_per_rank`` per step (weak scaling)."""
+    return world * units_per_rank * steps / seconds
+
+
 def run_gpu(args, rank, world):
     import torch
     from slakonet_gb300 import engine as E, model as M
@@ -251,10 +266,7 @@ def run_gpu(args, rank, world):
     for name, a, b in eng.event_log:
         per_call.setdefault(name, []).append(a.elapsed_time(b) * 1e-3)
     eng.event_log = None
-    if world > 1:
-        t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(elapsed, world, dev)
     ok = int((res.eig_status == 0).sum().item())
 
     log("end-to-end")
@@ -273,10 +285,7 @@ def run_gpu(args, rank, world):
         d2h = int(eig_h.numel() * 8 + dos_h.numel() * 8 + st_h.numel() * 8 + 4 * plan.n_pairs)
         h2d = E.DeviceBatch(r.plan, dev).h2d_bytes() + 8 * (2 * plan.n_pairs + 1)
     e2e = sum(e2e_times)
-    if world > 1:
-        t = torch.tensor([e2e], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e = float(t.item())
+    e2e = max_over_ranks(e2e, world, dev)
 
     peak = fp64_peak(torch, None, dev)
     eig_t = statistics.mean(per_call["eigensolve"])
@@ -285,7 +294,7 @@ def run_gpu(args, rank, world):
     if rank != 0:
         return None
     out = {
-        "metric": METRIC, "value": world * solves * args.steps / elapsed, "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": job_rate(world, solves, args.steps, elapsed), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "structures": args.structures, "seed": args.seed,
@@ -309,7 +318,7 @@ def run_gpu(args, rank, world):
                                     "8/3 n^3 per real one (2k integer: dpotrf + dsygst + dsytrd)",
                      "real_k_points": int(plan.prob_real.sum()),
                      "eig_kernel_ms": eig_t * 1e3, "time_share": shares},
-        "e2e": {"value": world * solves * args.steps / e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": job_rate(world, solves, args.steps, e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e / args.steps},
         "gpu_launches": launches,
         "clocks": clk.summary(),
