@@ -190,6 +190,17 @@ class Server:
                     if self.stop and not self.ready:
                         return
                 continue
+            # claim each future: one a client cancelled while it waited is dropped here (its memory
+            # released), and none can be cancelled once its batch runs
+            live = []
+            for r in batch:
+                if r.future.set_running_or_notify_cancel():
+                    live.append(r)
+                else:
+                    self.adm.release(r.nbytes)
+            batch = live
+            if not batch:
+                continue
             t0 = time.perf_counter()
             for r in batch:
                 r.t_start = t0

@@ -80,6 +80,70 @@ def test_batches_form_from_requests_that_arrive_during_execution():
     assert sizes[0] == 1 and max(sizes[1:]) > 1
 
 
+def _gated_server(fail_marker=None):
+    """One worker whose executor waits for ``gate`` and fails any batch holding ``fail_marker`` atoms."""
+    gate = threading.Event()
+    seen = []
+
+    def execute(structures, stream):
+        gate.wait(10)
+        seen.append([len(s["numbers"]) for s in structures])
+        if fail_marker is not None and any(len(s["numbers"]) == fail_marker for s in structures):
+            raise RuntimeError("simulated executor failure")
+        return [{"n": len(s["numbers"])} for s in structures]
+
+    server = SV.Server(FakeModel(), syn.default_shell_dict(), device="cpu", mem_budget_bytes=1 << 40,
+                       n_workers=1, executor=execute)
+    return server, gate, seen
+
+
+def _atoms(n):
+    return {"numbers": np.ones(n, dtype=np.int64), "positions": np.zeros((n, 3)), "cell": np.eye(3) * 10,
+            "kpoints": np.zeros((1, 3))}
+
+
+def _wait_for(pred, timeout=10.0):
+    t = time.time()
+    while not pred() and time.time() - t < timeout:
+        time.sleep(0.005)
+    assert pred()
+
+
+def test_executor_failure_reaches_every_request_of_its_batch_and_serving_continues():
+    server, gate, seen = _gated_server(fail_marker=7)
+    first = server.submit(_atoms(1))                    # occupies the worker until the gate opens
+    _wait_for(lambda: server.adm.used > 0 and not server.ready)
+    mix = [server.submit(_atoms(n)) for n in (2, 7, 3)]  # queued together behind it; 7 atoms fails the batch
+    _wait_for(lambda: len(server.ready) == 3)
+    gate.set()
+    assert first.result(timeout=10) == {"n": 1, "latency_s": first.result()["latency_s"]}
+    for f in mix:
+        with pytest.raises(RuntimeError, match="simulated executor failure"):
+            f.result(timeout=10)
+    after = server.submit(_atoms(4))
+    assert after.result(timeout=10)["n"] == 4             # the worker survived the failed batch
+    server.close()
+    assert seen == [[1], [2, 7, 3], [4]]
+    assert server.adm.used == 0                          # every request's memory was released
+
+
+def test_cancelled_request_is_dropped_before_execution_and_worker_survives():
+    server, gate, seen = _gated_server()
+    first = server.submit(_atoms(1))
+    _wait_for(lambda: server.adm.used > 0 and not server.ready)
+    cancelled, kept = server.submit(_atoms(5)), server.submit(_atoms(6))
+    _wait_for(lambda: len(server.ready) == 2)
+    assert cancelled.cancel()
+    gate.set()
+    assert first.result(timeout=10)["n"] == 1 and kept.result(timeout=10)["n"] == 6
+    assert cancelled.cancelled()
+    after = server.submit(_atoms(2))
+    assert after.result(timeout=10)["n"] == 2
+    server.close()
+    assert [5] not in seen and all(5 not in b for b in seen)
+    assert server.adm.used == 0
+
+
 _KEYS = ("numbers", "positions", "cell", "kpoints", "weights")
 
 
