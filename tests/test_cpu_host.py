@@ -104,6 +104,25 @@ def test_state_dict_layout_matches_reference_keys():
     assert p.dtype.is_floating_point and p.shape == (2, len(tables["grid"]))
 
 
+def test_state_dict_round_trip_reloads_values_and_repacks_tables():
+    import io
+    import torch
+    sd = {6: [0, 1], 14: [0, 1, 2]}
+    src = M.MultiElementSkfParameterOptimizer.from_tables(syn.make_tables([6, 14], sd, seed=0))
+    dst = M.MultiElementSkfParameterOptimizer.from_tables(syn.make_tables([6, 14], sd, seed=1))
+    before = dst.table_set(sd, "cpu")
+    buf = io.BytesIO()
+    torch.save(src.state_dict(), buf)
+    buf.seek(0)
+    dst.load_state_dict(torch.load(buf))
+    a, b = src.state_dict(), dst.state_dict()
+    assert a.keys() == b.keys() and all(torch.equal(a[k], b[k]) for k in a)
+    after = dst.table_set(sd, "cpu")                      # loading copies in place: the tables repack
+    assert after is not before
+    ref = src.table_set(sd, "cpu")
+    assert torch.equal(after.tab_H, ref.tab_H) and torch.equal(after.tab_S, ref.tab_S)
+
+
 def test_apply_constraints_clamps_to_band():
     tables = syn.make_tables([14], {14: [0, 1]}, seed=0)
     m = M.MultiElementSkfParameterOptimizer.from_tables(tables)
