@@ -127,14 +127,14 @@ def test_apply_constraints_clamps_to_band():
     tables = syn.make_tables([14], {14: [0, 1]}, seed=0)
     m = M.MultiElementSkfParameterOptimizer.from_tables(tables)
     p = m.skf_optimizers["Si-Si"].h_params["0-1"]
-    o = p.detach().clone()
+    o = p.detach().clone().numpy()
     with __import__("torch").no_grad():
         p.mul_(3.0)
     m.apply_constraints()
     lo = np.minimum(o * 0.7, o * 1.3)
     hi = np.maximum(o * 0.7, o * 1.3)
     v = p.detach().numpy()
-    assert (v >= lo.numpy() - 1e-15).all() and (v <= hi.numpy() + 1e-15).all()
+    assert (v >= lo - 1e-15).all() and (v <= hi + 1e-15).all()
 
 
 def test_engine_refuses_cpu():
