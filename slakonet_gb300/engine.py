@@ -171,6 +171,31 @@ class TableSet:
 
 # ---------------------------------------------------------------- planning
 
+# The bond search gives each ordered atom pair one GPU thread that loops over every lattice translation
+# of the structure's box, so its work is translations x atoms^2.  Both are bounded here: a 1 A cubic
+# cell needs ~2,200 translations; the 1000-atom 5x5x5 zincblende supercell needs 125 x 10^6.
+MAX_IMAGES = 1 << 20
+MAX_PAIR_IMAGES = 10 ** 11
+
+
+def _check_structure(s: int, z, p, c, k, w) -> None:
+    """Reject a structure whose arrays disagree in length or hold non-finite values.  Every flat
+    offset the kernels use comes from these lengths, so a mismatch must stop here, on the host."""
+    if len(z) == 0:
+        raise ValueError(f"structure {s}: no atoms")
+    if len(p) != len(z):
+        raise ValueError(f"structure {s}: {len(p)} positions for {len(z)} atoms")
+    if len(k) == 0:
+        raise ValueError(f"structure {s}: no k-points")
+    if len(w) != len(k):
+        raise ValueError(f"structure {s}: {len(w)} k-point weights for {len(k)} k-points")
+    for name, a in (("positions", p), ("cell", c), ("kpoints", k), ("weights", w)):
+        if not np.isfinite(a).all():
+            raise ValueError(f"structure {s}: non-finite {name}")
+    if abs(np.linalg.det(c)) <= 1e-12 * max(np.abs(c).max(), 1.0) ** 3:
+        raise ValueError(f"structure {s}: singular cell")
+
+
 def image_range(cell: np.ndarray, positions: np.ndarray, cutoff: float) -> np.ndarray:
     """Half-widths r of the translation box holding every bond shorter than cutoff.
 
@@ -232,6 +257,8 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
     The per-structure loop only gathers arrays and sizes the translation box;
     everything per atom or per orbital is built with whole-batch array operations."""
     S = len(structures)
+    if S == 0:
+        raise ValueError("empty batch: no structures")
     nums, pos, cells, kp, kw = [], [], [], [], []
     n_at = np.zeros(S, np.int64)
     nk = np.zeros(S, np.int32)
@@ -241,7 +268,8 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
         p = np.asarray(st["positions"], dtype=np.float64).reshape(-1, 3)
         c = np.asarray(st["cell"], dtype=np.float64).reshape(3, 3)
         k = np.asarray(st["kpoints"], dtype=np.float64).reshape(-1, 3)
-        w = np.asarray(st.get("weights", np.full(len(k), 1.0 / max(len(k), 1))), dtype=np.float64)
+        w = np.asarray(st.get("weights", np.full(len(k), 1.0 / max(len(k), 1))), dtype=np.float64).reshape(-1)
+        _check_structure(s, z, p, c, k, w)
         nums.append(z)
         pos.append(p)
         cells.append(c)
@@ -249,7 +277,13 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
         kw.append(w)
         n_at[s] = len(z)
         nk[s] = len(k)
-        rng[s] = image_range(c, p, cutoff)
+        r = image_range(c, p, cutoff)
+        n_img = int(np.prod(2 * r.astype(np.int64) + 1))
+        if n_img > MAX_IMAGES or n_img * len(z) ** 2 > MAX_PAIR_IMAGES:
+            raise ValueError(f"structure {s}: the cell is too small or too flat for the {cutoff:g} Bohr cutoff "
+                             f"({'x'.join(str(2 * int(x) + 1) for x in r)} translations for {len(z)} atoms; "
+                             f"at most {MAX_IMAGES} translations and {MAX_PAIR_IMAGES:.0e} atom-pair translations)")
+        rng[s] = r
     zall = np.concatenate(nums) if S else np.zeros(0, np.int64)
     lut = tables.__dict__.get("_species_lut")
     if lut is None:

@@ -238,3 +238,34 @@ def test_plan_batch_matches_per_structure_construction():
         a0 += N
         o0 += n
     assert plan.atom_ptr[-1] == a0 and plan.orb_ptr[-1] == o0
+
+
+def test_plan_rejects_malformed_structures_on_the_host():
+    """Every flat offset the kernels use comes from these lengths, and the bond search loops over every
+    lattice translation: malformed or degenerate input must stop in plan_batch, before any launch."""
+    sd = {6: [0, 1], 14: [0, 1, 2]}
+    ts = M.MultiElementSkfParameterOptimizer.from_tables(syn.make_tables([6, 14], sd, seed=0)).table_set(sd, "cpu")
+    ok = {"numbers": np.array([6, 14]), "positions": np.array([[0.0, 0, 0], [1.5, 1.5, 1.5]]),
+          "cell": np.eye(3) * 6.0, "kpoints": np.zeros((2, 3)), "weights": np.full(2, 0.5)}
+    E.plan_batch([ok], ts)
+    bad = {
+        "no atoms": dict(ok, numbers=np.zeros(0, np.int64), positions=np.zeros((0, 3))),
+        "positions for": dict(ok, positions=np.zeros((3, 3))),
+        "no k-points": dict(ok, kpoints=np.zeros((0, 3)), weights=np.zeros(0)),
+        "k-point weights": dict(ok, weights=np.ones(3)),
+        "non-finite positions": dict(ok, positions=np.array([[0.0, 0, 0], [np.nan, 0, 0]])),
+        "non-finite cell": dict(ok, cell=np.diag([6.0, np.inf, 6.0])),
+        "non-finite kpoints": dict(ok, kpoints=np.array([[0.0, 0, 0], [np.inf, 0, 0]])),
+        "singular cell": dict(ok, cell=np.array([[1.0, 0, 0], [2.0, 0, 0], [0, 0, 1.0]])),
+        "too small or too flat": dict(ok, cell=np.array([[6.0, 0, 0], [0, 6.0, 0], [0, 0, 1e-4]])),
+    }
+    for msg, st in bad.items():
+        with pytest.raises(ValueError, match=msg):
+            E.plan_batch([ok, st], ts)
+    with pytest.raises(ValueError, match="empty batch"):
+        E.plan_batch([], ts)
+    # the translation-times-pairs bound: 1000 atoms in a flat cell that alone would be allowed
+    many = dict(ok, numbers=np.full(1000, 6), positions=np.random.default_rng(0).uniform(0, 6, (1000, 3)),
+                cell=np.array([[6.0, 0, 0], [0, 6.0, 0], [0, 0, 0.005]]))
+    with pytest.raises(ValueError, match="atom-pair translations"):
+        E.plan_batch([many], ts)
