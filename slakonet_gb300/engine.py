@@ -178,9 +178,27 @@ MAX_IMAGES = 1 << 20
 MAX_PAIR_IMAGES = 10 ** 11
 
 
-def _check_structure(s: int, z, p, c, k, w) -> None:
-    """Reject a structure whose arrays disagree in length or hold non-finite values.  Every flat
-    offset the kernels use comes from these lengths, so a mismatch must stop here, on the host."""
+def check_structure(st: dict, cutoff: float = CUTOFF_BOHR, s: int = 0):
+    """One structure's arrays (numbers, positions, cell, kpoints, weights) and its translation box,
+    or ValueError when they disagree in length, hold non-finite values, or need an unbounded bond
+    search.  Every flat offset the kernels use comes from these lengths, so a bad structure must
+    stop here, on the host.  ``weights`` defaults to uniform."""
+    z = np.asarray(st["numbers"], dtype=np.int64).reshape(-1)
+    p = np.asarray(st["positions"], dtype=np.float64).reshape(-1, 3)
+    c = np.asarray(st["cell"], dtype=np.float64).reshape(3, 3)
+    k = np.asarray(st["kpoints"], dtype=np.float64).reshape(-1, 3)
+    w = np.asarray(st.get("weights", np.full(len(k), 1.0 / max(len(k), 1))), dtype=np.float64).reshape(-1)
+    _check_arrays(s, z, p, c, k, w)
+    r = image_range(c, p, cutoff)
+    n_img = int(np.prod(2 * r.astype(np.int64) + 1))
+    if n_img > MAX_IMAGES or n_img * len(z) ** 2 > MAX_PAIR_IMAGES:
+        raise ValueError(f"structure {s}: the cell is too small or too flat for the {cutoff:g} Bohr cutoff "
+                         f"({'x'.join(str(2 * int(x) + 1) for x in r)} translations for {len(z)} atoms; "
+                         f"at most {MAX_IMAGES} translations and {MAX_PAIR_IMAGES:.0e} atom-pair translations)")
+    return z, p, c, k, w, r
+
+
+def _check_arrays(s: int, z, p, c, k, w) -> None:
     if len(z) == 0:
         raise ValueError(f"structure {s}: no atoms")
     if len(p) != len(z):
@@ -264,12 +282,7 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
     nk = np.zeros(S, np.int32)
     rng = np.zeros((S, 3), np.int32)
     for s, st in enumerate(structures):
-        z = np.asarray(st["numbers"], dtype=np.int64).reshape(-1)
-        p = np.asarray(st["positions"], dtype=np.float64).reshape(-1, 3)
-        c = np.asarray(st["cell"], dtype=np.float64).reshape(3, 3)
-        k = np.asarray(st["kpoints"], dtype=np.float64).reshape(-1, 3)
-        w = np.asarray(st.get("weights", np.full(len(k), 1.0 / max(len(k), 1))), dtype=np.float64).reshape(-1)
-        _check_structure(s, z, p, c, k, w)
+        z, p, c, k, w, r = check_structure(st, cutoff, s)
         nums.append(z)
         pos.append(p)
         cells.append(c)
@@ -277,12 +290,6 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
         kw.append(w)
         n_at[s] = len(z)
         nk[s] = len(k)
-        r = image_range(c, p, cutoff)
-        n_img = int(np.prod(2 * r.astype(np.int64) + 1))
-        if n_img > MAX_IMAGES or n_img * len(z) ** 2 > MAX_PAIR_IMAGES:
-            raise ValueError(f"structure {s}: the cell is too small or too flat for the {cutoff:g} Bohr cutoff "
-                             f"({'x'.join(str(2 * int(x) + 1) for x in r)} translations for {len(z)} atoms; "
-                             f"at most {MAX_IMAGES} translations and {MAX_PAIR_IMAGES:.0e} atom-pair translations)")
         rng[s] = r
     zall = np.concatenate(nums) if S else np.zeros(0, np.int64)
     lut = tables.__dict__.get("_species_lut")

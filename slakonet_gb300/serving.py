@@ -105,16 +105,28 @@ class Server:
 
     # ------------------------------------------------------------ clients
     def submit(self, structure: dict) -> cf.Future:
-        n_orb = sum(sum(2 * l + 1 for l in self.sd[int(z)]) for z in np.asarray(structure["numbers"]).reshape(-1))
+        zs = np.asarray(structure["numbers"]).reshape(-1)
+        missing = sorted({int(z) for z in zs} - set(int(z) for z in self.sd))
+        n_orb = sum(sum(2 * l + 1 for l in self.sd[int(z)]) for z in zs) if not missing else 0
         nk = len(structure["kpoints"])
         with self.cv:
             self.rid += 1
             req = Request(self.rid, structure, n_orb, nk, request_bytes(n_orb, nk, self.dos["dos_points"]),
                           time.perf_counter())
-        if n_orb > MAX_N:
+        err = None
+        if missing:
+            err = ValueError(f"no shells for element Z={missing[0]}")
+        elif n_orb > MAX_N:
+            err = ValueError(f"{n_orb} orbitals exceed the eigensolver's {MAX_N}")
+        else:
+            try:   # a malformed structure is refused alone instead of failing the batch it would join
+                E.check_structure(structure)
+            except ValueError as e:
+                err = e
+        if err is not None:
             with self.cv:
                 self.rejected += 1
-            req.future.set_exception(ValueError(f"{n_orb} orbitals exceed the eigensolver's {MAX_N}"))
+            req.future.set_exception(err)
             return req.future
         self.pending.put(req)
         return req.future

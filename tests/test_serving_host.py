@@ -80,6 +80,24 @@ def test_batches_form_from_requests_that_arrive_during_execution():
     assert sizes[0] == 1 and max(sizes[1:]) > 1
 
 
+def test_malformed_requests_are_refused_alone_and_batch_mates_complete():
+    server, gate, seen = _gated_server()
+    good = [server.submit(_atoms(2)), server.submit(_atoms(3))]
+    bad = {"positions for": dict(_atoms(2), positions=np.zeros((3, 3))),
+           "k-point weights": dict(_atoms(2), weights=np.ones(4)),
+           "non-finite": dict(_atoms(2), cell=np.diag([10.0, np.nan, 10.0])),
+           "no shells for element": dict(_atoms(2), numbers=np.array([1, 200]))}
+    futs = {m: server.submit(st) for m, st in bad.items()}
+    gate.set()
+    for m, f in futs.items():
+        with pytest.raises(ValueError, match=m):
+            f.result(timeout=10)
+    assert [f.result(timeout=10)["n"] for f in good] == [2, 3]
+    server.close()
+    assert server.rejected == len(bad) and all(n in (2, 3) for b in seen for n in b)
+    assert server.adm.used == 0
+
+
 def _gated_server(fail_marker=None):
     """One worker whose executor waits for ``gate`` and fails any batch holding ``fail_marker`` atoms."""
     gate = threading.Event()
