@@ -191,6 +191,21 @@ def fp64_peak(torch, lib, dev):
     return best
 
 
+def hbm_context(traffic_bytes, seconds, peaks_path=os.path.join(ROOT, "MEASURED_PEAKS.json")):
+    """DRAM rate of one launch (ncu traffic / CUDA-event time) against the measured HBM copy peak,
+    or None when either number is missing."""
+    if not traffic_bytes or not seconds:
+        return None
+    try:
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError, TypeError):
+        return None
+    gbs = traffic_bytes / seconds / 1e9
+    return {"achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
+
 def max_over_ranks(x: float, world: int, device=None) -> float:
     """The largest ``x`` over all ranks: a job of replicas takes as long as its slowest rank."""
     if world <= 1:
@@ -317,6 +332,8 @@ def run_gpu(args, rank, world):
                      "algorithmic": "32/3 n^3 real flops per complex k-point (zpotrf 4/3 + zhegst 4 + zhetrd 16/3), "
                                     "8/3 n^3 per real one (2k integer: dpotrf + dsygst + dsytrd)",
                      "real_k_points": int(plan.prob_real.sum()),
+                     "hbm": hbm_context(EIG_TRAFFIC_BYTES if (args.structures, args.seed) == (N_STRUCT, SEED)
+                                        else None, eig_t),
                      "eig_kernel_ms": eig_t * 1e3, "time_share": shares},
         "e2e": {"value": job_rate(world, solves, args.steps, e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e / args.steps},

@@ -1,4 +1,4 @@
-"""Multi-rank host logic of bench.py on CPU (gloo, world size 2).
+"""Host logic of bench.py on CPU: the multi-rank path (gloo, world size 2) and the roofline context.
 
 Every rank of ``bench.py --gpus N`` is an independent replica of the whole
 workload; ranks meet only at barriers and at the max-over-ranks reduction
@@ -67,3 +67,13 @@ def test_reference_arm_other_ranks_exit_without_work():
                        env=env, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_hbm_context_against_measured_peak(tmp_path):
+    bench = _bench()
+    peaks = tmp_path / "peaks.json"
+    peaks.write_text(json.dumps({"hbm_gbs": 6000.0}))
+    h = bench.hbm_context(1.5e12, 1.0, str(peaks))
+    assert h["achieved_gbs"] == 1500.0 and h["peak_gbs"] == 6000.0 and h["frac"] == 0.25
+    assert bench.hbm_context(None, 1.0, str(peaks)) is None
+    assert bench.hbm_context(1.5e12, 1.0, str(tmp_path / "absent.json")) is None
