@@ -191,19 +191,39 @@ def fp64_peak(torch, lib, dev):
     return best
 
 
-def hbm_context(traffic_bytes, seconds, peaks_path=os.path.join(ROOT, "MEASURED_PEAKS.json")):
-    """DRAM rate of one launch (ncu traffic / CUDA-event time) against the measured HBM copy peak,
-    or None when either number is missing."""
-    if not traffic_bytes or not seconds:
-        return None
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def measured_hbm_gbs(peaks_path=PEAKS_PATH):
+    """The measured HBM copy bandwidth (GB/s), or None when the file is absent or unreadable."""
     try:
         with open(peaks_path) as f:
-            peak = float(json.load(f)["hbm_gbs"])
+            return float(json.load(f)["hbm_gbs"])
     except (OSError, ValueError, KeyError, TypeError):
+        return None
+
+
+def hbm_context(traffic_bytes, seconds, peaks_path=PEAKS_PATH):
+    """DRAM rate of one launch (ncu traffic / CUDA-event time) against the measured HBM copy peak,
+    or None when either number is missing."""
+    peak = measured_hbm_gbs(peaks_path)
+    if not traffic_bytes or not seconds or not peak:
         return None
     gbs = traffic_bytes / seconds / 1e9
     return {"achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
+
+def bloch_roofline(seconds_per_step, hs_total, peaks_path=PEAKS_PATH):
+    """k_bloch is bound by its HBM writes: H(k) and S(k), 16 bytes per complex element each, so
+    2 * 16 * (sum of n^2 over the step's problems) algorithmic bytes per step."""
+    if not seconds_per_step:
+        return None
+    nbytes = 2 * 16 * int(hs_total)
+    gbs = nbytes / seconds_per_step / 1e9
+    peak = measured_hbm_gbs(peaks_path)
+    return {"bound": "hbm", "bytes_per_step": nbytes, "ms_per_step": 1e3 * seconds_per_step, "achieved_gbs": gbs,
+            "peak_gbs": peak, "frac": (gbs / peak) if peak else None}
 
 
 def max_over_ranks(x: float, world: int, device=None) -> float:
@@ -334,6 +354,8 @@ def run_gpu(args, rank, world):
                      "real_k_points": int(plan.prob_real.sum()),
                      "hbm": hbm_context(EIG_TRAFFIC_BYTES if (args.structures, args.seed) == (N_STRUCT, SEED)
                                         else None, eig_t),
+                     "stages": {"bloch": bloch_roofline(sum(per_call.get("skn_bloch", [])) / args.steps,
+                                                        plan.hs_total)},
                      "eig_kernel_ms": eig_t * 1e3, "time_share": shares},
         "e2e": {"value": job_rate(world, solves, args.steps, e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e / args.steps},

@@ -77,3 +77,13 @@ def test_hbm_context_against_measured_peak(tmp_path):
     assert h["achieved_gbs"] == 1500.0 and h["peak_gbs"] == 6000.0 and h["frac"] == 0.25
     assert bench.hbm_context(None, 1.0, str(peaks)) is None
     assert bench.hbm_context(1.5e12, 1.0, str(tmp_path / "absent.json")) is None
+
+
+def test_bloch_roofline_counts_h_and_s_writes(tmp_path):
+    bench = _bench()
+    peaks = tmp_path / "peaks.json"
+    peaks.write_text(json.dumps({"hbm_gbs": 8000.0}))
+    r = bench.bloch_roofline(0.004, 10 ** 8, str(peaks))        # 2 * 16 bytes * 1e8 elements in 4 ms
+    assert r["bytes_per_step"] == 32 * 10 ** 8 and r["achieved_gbs"] == 800.0 and r["frac"] == 0.1
+    assert bench.bloch_roofline(0.0, 10 ** 8, str(peaks)) is None
+    assert bench.bloch_roofline(0.004, 10 ** 8, str(tmp_path / "absent.json"))["frac"] is None
