@@ -8,10 +8,12 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import threading
 
 from . import build as _build
 
 _LIB = None
+_LOAD_LOCK = threading.Lock()   # server workers can make their first call at the same time
 
 SKN_OK = 0
 SKN_ERR_ARG = 1
@@ -74,18 +76,21 @@ def load(build_if_missing: bool = True):
     global _LIB
     if _LIB is not None:
         return _LIB
-    path = lib_path()
-    if not os.path.exists(path) or _build._stale():
-        if not build_if_missing:
-            raise SknError(f"CUDA library not built: {path}")
-        _build.build()
-    lib = C.CDLL(path)
-    for name, argt in SIGNATURES.items():
-        fn = getattr(lib, name)
-        fn.argtypes = argt
-        fn.restype = C.c_int
-    _LIB = lib
-    return lib
+    with _LOAD_LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = lib_path()
+        if not os.path.exists(path) or _build._stale():
+            if not build_if_missing:
+                raise SknError(f"CUDA library not built: {path}")
+            _build.build()
+        lib = C.CDLL(path)
+        for name, argt in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = argt
+            fn.restype = C.c_int
+        _LIB = lib
+        return lib
 
 
 def call(name: str, *args):

@@ -7,6 +7,7 @@ header is newer than the library.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import fcntl
 import glob
 import os
 import shutil
@@ -45,9 +46,20 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile every translation unit for sm_103a and link the in-tree shared library (skipped when it
+    is newer than every source).  Processes that build at the same time take turns on a lock file, and
+    one that waited finds the library built."""
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
+    with open(os.path.join(BUILD, ".build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and not _stale():
+            return LIB
+        return _build_locked(verbose)
+
+
+def _build_locked(verbose: bool) -> str:
     cc = nvcc()
     inc = ["-I", os.path.join(ROOT, "include")]
 
