@@ -37,7 +37,6 @@ def compute_atom_projected_dos(properties, geometry, sigma=0.1, energy_range=(-8
     ev = calc.eigenvectors                       # [1, n_orb, nb, nk]
     eig = torch.as_tensor(calc.eigenvalue)       # [1, nk, nb], Hartree
     dev = ev.device if ev.is_cuda else torch.device("cuda")
-    _lib.load()
     atom_types = _atom_types(geometry)
     unique = list(dict.fromkeys(atom_types))
     n_orb = int(ev.shape[1])
@@ -47,6 +46,11 @@ def compute_atom_projected_dos(properties, geometry, sigma=0.1, energy_range=(-8
     per = n_orb // n_atoms
     group = np.repeat(np.array([unique.index(a) for a in atom_types], dtype=np.int32), per)
     nk, nb = int(eig.shape[1]), int(eig.shape[2])
+    if eig.dim() != 3 or tuple(ev.shape) != (1, n_orb, nb, nk):
+        # the kernel indexes the eigenvectors with the eigenvalue array's sizes
+        raise ValueError(f"eigenvectors {tuple(ev.shape)} do not match eigenvalues {tuple(eig.shape)}: "
+                         f"expected [1, n_orbitals, n_bands, n_kpoints] = [1, {n_orb}, {nb}, {nk}]")
+    _lib.load()
     with torch.cuda.device(dev):
         vec = ev[0].permute(2, 0, 1).to(device=dev, dtype=torch.complex128).contiguous()   # [nk, n_orb, nb]
         e = eig[0].to(device=dev, dtype=torch.float64).contiguous()

@@ -269,3 +269,14 @@ def test_plan_rejects_malformed_structures_on_the_host():
                 cell=np.array([[6.0, 0, 0], [0, 6.0, 0], [0, 0, 0.005]]))
     with pytest.raises(ValueError, match="atom-pair translations"):
         E.plan_batch([many], ts)
+
+
+def test_atom_projected_dos_rejects_mismatched_shapes_before_launch():
+    import types
+    import torch
+    from slakonet_gb300 import compute_atom_projected_dos
+    geom = M.Geometry([14, 14], np.zeros((2, 3)), np.eye(3) * 10)
+    calc = types.SimpleNamespace(eigenvalue=torch.zeros(1, 3, 8),                     # nk 3, 8 bands
+                                 eigenvectors=torch.zeros(1, 8, 8, 2, dtype=torch.complex128))   # nk 2
+    with pytest.raises(ValueError, match="do not match"):
+        compute_atom_projected_dos({"fermi_energy_eV": 0.0, "calc": calc}, geom)
