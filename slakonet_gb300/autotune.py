@@ -149,7 +149,7 @@ def autotune(device="cuda", cache: Optional[str] = None, budget_s: float = 0.04,
     key = _cache_key(device)
     if use_cache and os.path.exists(cache):
         try:
-            data = json.load(open(cache))
+            data = _read_cache(cache)
             want = set(buckets or BUCKETS)
             if key in data and want <= {int(k) for k in data[key]["choice"]}:
                 return Tuning(data[key]["choice"], data[key].get("timings"))
@@ -167,18 +167,33 @@ def autotune(device="cuda", cache: Optional[str] = None, budget_s: float = 0.04,
         timings[str(u)] = {(sfx or "_t128"): round(v * 1e3, 3) for sfx, v in t.items()}
     tun = Tuning(choice, timings)
     try:
-        os.makedirs(os.path.dirname(cache), exist_ok=True)
-        data = json.load(open(cache)) if os.path.exists(cache) else {}
-        if key in data:          # merge with buckets tuned earlier
-            merged = {int(k): v for k, v in data[key]["choice"].items()}
-            merged.update(tun.choice)
-            mt = dict(data[key].get("timings", {}))
-            mt.update(tun.timings)
-            tun = Tuning(merged, mt)
-        data[key] = tun.to_json()
-        json.dump(data, open(cache, "w"), indent=1)
-    except (OSError, ValueError):
+        tun = _merge_into_cache(cache, key, tun)
+    except (OSError, ValueError, KeyError):
         pass
+    return tun
+
+
+def _read_cache(path: str) -> dict:
+    with open(path) as f:
+        return json.load(f)
+
+
+def _merge_into_cache(path: str, key: str, tun: Tuning) -> Tuning:
+    """Merge ``tun`` with the buckets tuned earlier under ``key`` and write the cache through a
+    temporary file, so a reader never sees a partly written file.  Returns the merged tuning."""
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    data = _read_cache(path) if os.path.exists(path) else {}
+    if key in data:
+        merged = {int(k): v for k, v in data[key]["choice"].items()}
+        merged.update(tun.choice)
+        mt = dict(data[key].get("timings", {}))
+        mt.update(tun.timings)
+        tun = Tuning(merged, mt)
+    data[key] = tun.to_json()
+    tmp = f"{path}.{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        json.dump(data, f, indent=1)
+    os.replace(tmp, path)
     return tun
 
 

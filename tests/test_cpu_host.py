@@ -280,3 +280,22 @@ def test_atom_projected_dos_rejects_mismatched_shapes_before_launch():
                                  eigenvectors=torch.zeros(1, 8, 8, 2, dtype=torch.complex128))   # nk 2
     with pytest.raises(ValueError, match="do not match"):
         compute_atom_projected_dos({"fermi_energy_eV": 0.0, "calc": calc}, geom)
+
+
+def test_autotune_buckets_policies_and_cache_merge(tmp_path):
+    from slakonet_gb300 import autotune as AT
+    assert AT.buckets_up_to(492) == [16, 32, 64, 128, 256, 512]
+    assert AT.buckets_up_to(16) == [16] and AT.buckets_up_to(5000) == AT.BUCKETS
+    t = AT.Tuning({16: "_t64", 512: "_t256"})
+    assert [t.shape_for(n) for n in (1, 16, 17, 300, 512, 513, 9000)] == ["_t64", "_t64", "", "_t256", "_t256", "", ""]
+    pols = AT.candidate_policies(t)
+    assert pols[0].choice == AT.Tuning.default().choice and pols[-1] is t and len(pols) == 6
+    assert all(set(p.choice) == set(AT.BUCKETS) for p in pols[:-1])
+    path = str(tmp_path / "cache" / "autotune.json")
+    AT._merge_into_cache(path, "gpu-a", AT.Tuning({16: "_t64"}, {"16": {"_t64": 1.0}}))
+    merged = AT._merge_into_cache(path, "gpu-a", AT.Tuning({512: "_t256"}, {"512": {"_t256": 2.0}}))
+    assert merged.choice == {16: "_t64", 512: "_t256"} and set(merged.timings) == {"16", "512"}
+    AT._merge_into_cache(path, "gpu-b", AT.Tuning({32: ""}))
+    data = AT._read_cache(path)
+    assert set(data) == {"gpu-a", "gpu-b"} and data["gpu-a"]["choice"] == {"16": "_t64", "512": "_t256"}
+    assert not [f for f in os.listdir(os.path.dirname(path)) if f.endswith(".tmp")]
