@@ -94,6 +94,7 @@ class Server:
         self.ready: List[Request] = []                            # admitted, not started
         self.cv = threading.Condition()
         self.stop = False
+        self.closing = False
         self.rid = 0
         self.workers = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(n_workers)]
         self.admitter = threading.Thread(target=self._admit_loop, daemon=True)
@@ -123,22 +124,29 @@ class Server:
                 E.check_structure(structure)
             except ValueError as e:
                 err = e
-        if err is not None:
-            with self.cv:
-                self.rejected += 1
-            req.future.set_exception(err)
-            return req.future
-        self.pending.put(req)
+        with self.cv:
+            if err is None and self.closing:
+                err = RuntimeError("the server is closed")
+            if err is None:
+                self.pending.put(req)      # under the lock, so close() cannot slip in between
+                return req.future
+            self.rejected += 1
+        req.future.set_exception(err)
         return req.future
 
     def close(self):
+        """Refuse new requests, finish every request already submitted, then stop the threads."""
         with self.cv:
-            self.stop = True
+            if self.closing:
+                return
+            self.closing = True
+        self.pending.put(None)             # the admitter admits everything queued before this, then exits
+        self.admitter.join()
+        with self.cv:
+            self.stop = True               # workers exit once the ready list is empty
             self.cv.notify_all()
-        self.pending.put(None)
         for w in self.workers:
             w.join()
-        self.admitter.join()
 
     # ------------------------------------------------------------ internals
     def _admit_loop(self):

@@ -98,6 +98,26 @@ def test_malformed_requests_are_refused_alone_and_batch_mates_complete():
     assert server.adm.used == 0
 
 
+def test_close_finishes_every_submitted_request_and_refuses_new_ones():
+    def slow(structures, stream):
+        time.sleep(0.01)
+        return [{"n": len(s["numbers"])} for s in structures]
+
+    # room for about two requests at a time, so most of them still wait for admission at close()
+    budget = 2 * SV.request_bytes(4, 1, 1000) + 1
+    server = SV.Server(FakeModel(), syn.default_shell_dict(), device="cpu", mem_budget_bytes=budget, n_workers=2,
+                       executor=slow)
+    futs = [server.submit(_atoms(1 + i % 3)) for i in range(29)]
+    server.close()
+    assert all(f.done() for f in futs)
+    assert [f.result()["n"] for f in futs] == [1 + i % 3 for i in range(29)]
+    late = server.submit(_atoms(2))
+    with pytest.raises(RuntimeError, match="closed"):
+        late.result(timeout=1)
+    server.close()                                       # a second close is a no-op
+    assert server.adm.used == 0
+
+
 def _gated_server(fail_marker=None):
     """One worker whose executor waits for ``gate`` and fails any batch holding ``fail_marker`` atoms."""
     gate = threading.Event()
