@@ -214,6 +214,21 @@ def _check_arrays(s: int, z, p, c, k, w) -> None:
         raise ValueError(f"structure {s}: singular cell")
 
 
+INT32_LIMIT = 2 ** 31 - 1
+
+
+def _check_index_range(n_at, orb_cum, nk, orb_ptr64) -> None:
+    """The descriptor arrays hold batch-wide atom, orbital and k-point offsets in int32, and the
+    Fermi/DOS kernels index one structure's nk x n_orbitals eigenvalues with an int."""
+    if int(n_at.sum()) > INT32_LIMIT or int(orb_cum[-1]) > INT32_LIMIT or int(nk.astype(np.int64).sum()) > INT32_LIMIT:
+        raise ValueError("batch too large: its atoms, orbitals and k-points must each total below 2^31")
+    rows = nk.astype(np.int64) * np.diff(orb_ptr64).astype(np.int64)
+    if (rows > INT32_LIMIT).any():
+        s = int(np.argmax(rows > INT32_LIMIT))
+        raise ValueError(f"structure {s}: {int(nk[s])} k-points x {int(rows[s] // max(int(nk[s]), 1))} orbitals "
+                         "exceeds 2^31 eigenvalues")
+
+
 def image_range(cell: np.ndarray, positions: np.ndarray, cutoff: float) -> np.ndarray:
     """Half-widths r of the translation box holding every bond shorter than cutoff.
 
@@ -307,6 +322,7 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
     atom_ptr[1:] = np.cumsum(n_at)
     atom_struct = np.repeat(np.arange(S), n_at)
     orb_cum = np.concatenate([[0], np.cumsum(norb, dtype=np.int64)])
+    _check_index_range(n_at, orb_cum, nk, orb_cum[atom_ptr])
     orb_ptr = orb_cum[atom_ptr].astype(np.int32)
     nb = np.diff(orb_ptr).astype(np.int32)
     aoff = (orb_cum[:-1] - orb_ptr[atom_struct]).astype(np.int32)            # first local orbital per atom

@@ -299,3 +299,14 @@ def test_autotune_buckets_policies_and_cache_merge(tmp_path):
     data = AT._read_cache(path)
     assert set(data) == {"gpu-a", "gpu-b"} and data["gpu-a"]["choice"] == {"16": "_t64", "512": "_t256"}
     assert not [f for f in os.listdir(os.path.dirname(path)) if f.endswith(".tmp")]
+
+
+def test_index_range_guard_rejects_int32_overflow():
+    n_at = np.array([2, 3])
+    orb_cum = np.array([0, 4, 8, 13, 17, 21], dtype=np.int64)
+    E._check_index_range(n_at, orb_cum, np.array([10, 20], np.int32), np.array([0, 8, 21], np.int64))
+    with pytest.raises(ValueError, match="exceeds 2"):
+        E._check_index_range(n_at, orb_cum, np.array([1, 300_000_000], np.int32), np.array([0, 8, 21], np.int64))
+    with pytest.raises(ValueError, match="batch too large"):
+        E._check_index_range(n_at, np.array([0, 2 ** 31], np.int64), np.array([1, 1], np.int32),
+                             np.array([0, 1, 2], np.int64))
