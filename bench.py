@@ -56,6 +56,12 @@ WORKLOAD = ("uneven batch: 256 random periodic structures, 2-64 atoms log-unifor
 _T0 = time.perf_counter()
 
 
+def ordinal(n: int) -> str:
+    """1st, 2nd, 3rd, 4th, ..., 11th, 12th, 13th, ..., 21st, 22nd, 32nd."""
+    suffix = "th" if 10 <= n % 100 <= 20 else {1: "st", 2: "nd", 3: "rd"}.get(n % 10, "th")
+    return f"{n}{suffix}"
+
+
 def log(msg):
     sys.stderr.write(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}\n")
     sys.stderr.flush()
@@ -538,7 +544,7 @@ def run_reference_gpu(dev, sts, tables, sd, stride=32, limit=8):
         tot_t += dt
     return {"value": tot_k / tot_t, "unit": UNIT, "structures": len(sample), "k_point_solves": tot_k,
             "seconds": tot_t, "per_structure": per,
-            "sample": f"every {stride}th structure by size, first {limit}; the reference's "
+            "sample": f"every {ordinal(stride)} structure by size, first {limit}; the reference's "
                       "compute_multi_element_properties(device='cuda', get_fermi=True), one structure per call"}
 
 
@@ -625,7 +631,7 @@ def run_cpu_baseline(sts, tables, sd, reps=1):
             v = solves / sec
             best = v if best is None else max(best, v)
     return {"value": best, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"every {SAMPLE_STRIDE}th structure by size ({len(sample)} structures, {solves} k-point "
+            "sample": f"every {ordinal(SAMPLE_STRIDE)} structure by size ({len(sample)} structures, {solves} k-point "
                       f"solves, {sec:.1f} s), numpy/LAPACK oracle, one process per core"}
 
 
@@ -652,7 +658,7 @@ def run_reference(args):
             "config": {"workload": WORKLOAD, "structures": args.structures, "seed": args.seed,
                        "sample_structures": len(sample)},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"every {2 * SAMPLE_STRIDE}th structure by size ({len(sample)} structures,"
+                             "sample": f"every {ordinal(2 * SAMPLE_STRIDE)} structure by size ({len(sample)} structures,"
                                        f" {tot_s // max(args.steps, 1)} k-point solves per step)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

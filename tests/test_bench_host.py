@@ -87,3 +87,9 @@ def test_bloch_roofline_counts_h_and_s_writes(tmp_path):
     assert r["bytes_per_step"] == 32 * 10 ** 8 and r["achieved_gbs"] == 800.0 and r["frac"] == 0.1
     assert bench.bloch_roofline(0.0, 10 ** 8, str(peaks)) is None
     assert bench.bloch_roofline(0.004, 10 ** 8, str(tmp_path / "absent.json"))["frac"] is None
+
+
+def test_ordinal_suffixes():
+    bench = _bench()
+    assert [bench.ordinal(n) for n in (1, 2, 3, 4, 11, 12, 13, 16, 21, 22, 23, 32, 101, 111)] == \
+        ["1st", "2nd", "3rd", "4th", "11th", "12th", "13th", "16th", "21st", "22nd", "23rd", "32nd", "101st", "111th"]
