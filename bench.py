@@ -83,16 +83,19 @@ def orbitals(st, sd):
 
 
 # --------------------------------------------------------------- CPU side
+#
+# Both CPU legs (the GPU arm's cpu_baseline and the --impl reference arm) run the oracle on the same
+# stratified sample of the workload.  The work is cut into items -- each structure's real-space blocks
+# once, then (structure, k-chunk) Bloch sums and eigensolves, largest first -- so every host core stays
+# busy until the end; each worker process builds the whole seeded workload once when it starts (the
+# synthetic tables come from one sequential generator over the element list, so rebuilding them is exact
+# and avoids shipping ~300 MB of tables with every item).
 
-def _oracle_one(args):
-    st, tables, sd = args
-    from oracle import slako_oracle as O
-    r = O.run_structure(st, tables, sd, st["kpoints"], st["weights"], dos_range=DOS_RANGE,
-                        dos_points=DOS_POINTS, dos_sigma=DOS_SIGMA)
-    return len(st["kpoints"])
+K_CHUNK = 8                # k-points per CPU work item
+_W = {}                    # per worker process: the workload
 
 
-def _pool_init():
+def _pool_init(n_struct=None, seed=None):
     os.environ["OMP_NUM_THREADS"] = "1"
     os.environ["OPENBLAS_NUM_THREADS"] = "1"
     try:
@@ -100,26 +103,132 @@ def _pool_init():
         threadpool_limits(1)
     except Exception:
         pass
+    if n_struct is not None:
+        _W["sts"], _W["tables"], _W["sd"] = workload(n_struct, seed)
+
+
+def _oracle_blocks(item):
+    """The k-independent real-space blocks of one structure, for H or S (oracle)."""
+    idx, kind = item
+    from oracle import slako_oracle as O
+    return idx, kind, O.real_space_blocks(_W["sts"][idx], _W["tables"], _W["sd"], kind=kind)
+
+
+def _oracle_chunk(item):
+    """Bloch sums and eigenvalues of one k-chunk of one structure (oracle, one BLAS thread)."""
+    idx, c0, c1, blocks = item
+    from oracle import slako_oracle as O
+    st = _W["sts"][idx]
+    H, S = O.hk_sk(st, _W["tables"], _W["sd"], np.asarray(st["kpoints"])[c0:c1], blocks=blocks)
+    return idx, c0, O.eigh_generalized(H, S)
+
+
+def cpu_sample_indices(sts, stride=SAMPLE_STRIDE):
+    """Every ``stride``-th structure of the workload ordered by atom count, largest first."""
+    order = sorted(range(len(sts)), key=lambda i: -len(sts[i]["numbers"]))
+    return order[::stride]
 
 
 def cpu_sample(sts, stride=SAMPLE_STRIDE):
-    order = sorted(range(len(sts)), key=lambda i: -len(sts[i]["numbers"]))
-    return [sts[i] for i in order[::stride]]
+    return [sts[i] for i in cpu_sample_indices(sts, stride)]
 
 
-def time_oracle(sample, tables, sd, pool, cores):
-    """Returns (solves, seconds) for one pass of the oracle over the sample."""
-    sub_tables = tables
+def oracle_items(sts, idx, sd, chunk=K_CHUNK):
+    """(structure, k-chunk) work items of the sample, the costliest (n^3 x chunk length) first."""
+    items = []
+    for i in idx:
+        nk = len(sts[i]["kpoints"])
+        for c0 in range(0, nk, chunk):
+            items.append((i, c0, min(nk, c0 + chunk)))
+    n = {i: orbitals(sts[i], sd) for i in idx}
+    items.sort(key=lambda t: -(n[t[0]] ** 3) * (t[2] - t[1]))
+    return items
+
+
+def time_oracle(sts, idx, tables, sd, pool, props=True):
+    """One pass of the oracle over the sample ``idx``.  Stage 1 builds every structure's real-space H and
+    S blocks (one work item each, largest structure first); as soon as both of a structure's blocks are
+    back, its (structure, k-chunk) items -- Bloch sums and eigensolves -- join the queue.  Then, per
+    structure, the Fermi level, gap, band statistics and the DOS on the workload's grid (in this process).
+    Returns (k-point solves, seconds, {structure index: oracle properties incl. eigenvalues})."""
+    import queue
+    from oracle import slako_oracle as O
+    items = oracle_items(sts, idx, sd)
+    chunks = {i: [it for it in items if it[0] == i] for i in idx}
+    done_q = queue.Queue()
     t0 = time.perf_counter()
-    solves = sum(pool.imap_unordered(_oracle_one, [(st, sub_tables, sd) for st in sample], chunksize=1))
-    return solves, time.perf_counter() - t0
+    for i in idx:                                   # idx is largest first
+        for kind in ("H", "S"):
+            pool.apply_async(_oracle_blocks, ((i, kind),), callback=lambda r: done_q.put(("blocks", r)),
+                             error_callback=lambda e: done_q.put(("error", e)))
+    blocks = {i: {} for i in idx}
+    parts = {i: {} for i in idx}
+    left = len(items)
+    while left:
+        what, r = done_q.get()
+        if what == "error":
+            raise r
+        if what == "blocks":
+            i, kind, b = r
+            blocks[i][kind] = b
+            if len(blocks[i]) == 2:
+                bl = (blocks[i]["H"], blocks[i]["S"])
+                for (_, c0, c1) in chunks[i]:
+                    pool.apply_async(_oracle_chunk, ((i, c0, c1, bl),), callback=lambda r: done_q.put(("eig", r)),
+                                     error_callback=lambda e: done_q.put(("error", e)))
+        else:
+            i, c0, eig = r
+            parts[i][c0] = eig
+            left -= 1
+    out = {}
+    for i in idx:
+        eig = np.concatenate([parts[i][c] for c in sorted(parts[i])])
+        st = sts[i]
+        p = O.properties(eig, st["weights"], O.n_electrons(st["numbers"], tables), DOS_RANGE, DOS_POINTS,
+                         DOS_SIGMA) if props else {}
+        p["eigenvalues"] = eig
+        out[i] = p
+    sec = time.perf_counter() - t0
+    return sum(len(sts[i]["kpoints"]) for i in idx), sec, out
 
 
-def sub_tables_for(sample, tables):
-    zs = {int(z) for st in sample for z in st["numbers"]}
-    return {"grid": tables["grid"], "step": tables["step"],
-            "elements": {z: v for z, v in tables["elements"].items() if z in zs},
-            "pairs": {k: v for k, v in tables["pairs"].items() if k[0] in zs and k[1] in zs}}
+def oracle_pool(n_struct, seed, cores):
+    """Spawned pool of ``cores`` one-thread workers, each holding the seeded workload."""
+    _single_thread_workers()
+    return mp.get_context("spawn").Pool(cores, initializer=_pool_init, initargs=(n_struct, seed))
+
+
+def parity_against_oracle(res, idx, oracle, stat_index):
+    """Largest differences between the GPU results of a timed step and the oracle on the sample:
+    eigenvalues (eV, all structures), Fermi level and gap (eV, structures whose oracle Fermi search
+    converged) and DOS (states/eV, max abs).  ``res`` is the step's BatchResult, ``idx`` the sample's
+    structure indices in that batch, ``oracle`` the properties from ``time_oracle``."""
+    H2E = 27.211
+    stats = res.stats.cpu().numpy()
+    dos = res.dos.cpu().numpy()
+    e_eig = e_ef = e_gap = e_dos = 0.0
+    conv, not_conv, nan = [], [], []
+    for i in idx:
+        o = oracle[i]
+        g = res.eigenvalues(i).cpu().numpy()
+        if not (np.isfinite(g).all() and np.isfinite(o["eigenvalues"]).all()):
+            nan.append(int(i))
+            continue
+        e_eig = max(e_eig, float(np.abs(g - o["eigenvalues"]).max()) * H2E)
+        e_dos = max(e_dos, float(np.abs(dos[i] - o["dos_values"]).max()))
+        if o["fermi_converged"]:
+            conv.append(int(i))
+            e_ef = max(e_ef, abs(float(stats[i, stat_index["fermi_ev"]]) - o["fermi_energy_eV"]))
+            e_gap = max(e_gap, abs(float(stats[i, stat_index["gap_ev"]]) - o["band_gap_eV"]))
+        else:
+            not_conv.append(int(i))
+    return {"eig_max_eV": e_eig, "fermi_max_eV": e_ef if conv else None, "gap_max_eV": e_gap if conv else None,
+            "dos_max_abs": e_dos, "structures": len(idx), "k_point_solves": int(sum(len(oracle[i]["eigenvalues"])
+                                                                                   for i in idx)),
+            "fermi_gap_compared_on": len(conv), "oracle_fermi_not_converged": not_conv, "non_finite": nan,
+            "gates": {"eig_eV": 1e-8, "fermi_gap_eV": 1e-6, "dos_max_abs": 1e-6},
+            "reference": "CPU oracle (numpy/LAPACK restatement of the reference path) on the cpu_baseline sample, "
+                         "against the GPU results of the last timed step"}
 
 
 # --------------------------------------------------------------- clocks
@@ -175,26 +284,52 @@ class ClockSampler:
 
 # --------------------------------------------------------------- GPU arm
 
-def fp64_peak(torch, lib, dev):
-    """Measured FP64 FMA throughput (TFLOP/s) with the library's probe kernel."""
+def fp64_peak(torch, lib, dev, kind="fma"):
+    """Measured FP64 throughput (TFLOP/s) with the library's probe kernels: ``fma`` times FP64 fused
+    multiply-adds (16 flops per thread per step), ``dmma`` the FP64 tensor instruction mma.sync m8n8k4
+    (8 chains x 512 flops per warp per step)."""
     from slakonet_gb300._lib import call, ptr
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    blocks, iters = sms * 8, 4096
+    blocks = sms * 8
+    iters = 4096 if kind == "fma" else 256
+    name = "skn_fp64_probe" if kind == "fma" else "skn_fp64_probe_dmma"
+    flops = (16.0 * iters * blocks * 256) if kind == "fma" else (512.0 * 8 * iters * blocks * 8)
     out = torch.empty(blocks * 256, dtype=torch.float64, device=dev)
     s = torch.cuda.current_stream().cuda_stream
-    call("skn_fp64_probe", ptr(out), blocks, iters, s)
+    call(name, ptr(out), blocks, iters, s)
     torch.cuda.synchronize()
     best = 0.0
     for _ in range(3):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
-        call("skn_fp64_probe", ptr(out), blocks, iters, s)
+        call(name, ptr(out), blocks, iters, s)
         b.record()
         torch.cuda.synchronize()
         sec = a.elapsed_time(b) * 1e-3
-        best = max(best, 16.0 * iters * blocks * 256 / sec / 1e12)
+        best = max(best, flops / sec / 1e12)
     return best
+
+
+def time_sample_on_gpu(torch, eng, E, sts, idx, ts, dev, steps, kw):
+    """Device-resident solves/s of the whole path on the structures ``idx`` alone (the CPU legs' sample),
+    two warm-ups then ``steps`` timed executions, CUDA events on the current stream."""
+    plan = E.plan_batch([sts[i] for i in idx], ts)
+    db = E.DeviceBatch(plan, dev)
+    for _ in range(2):
+        eng.execute(db, **kw)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        eng.execute(db, **kw)
+    b.record()
+    torch.cuda.synchronize()
+    sec = a.elapsed_time(b) * 1e-3
+    solves = int(plan.nk.sum())
+    return {"value": solves * steps / sec, "unit": UNIT, "structures": len(idx), "k_point_solves": solves,
+            "ms_per_step": 1e3 * sec / steps}
 
 
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -328,7 +463,12 @@ def run_gpu(args, rank, world):
     e2e = sum(e2e_times)
     e2e = max_over_ranks(e2e, world, dev)
 
+    log("same-sample GPU figures")
+    on_cpu_sample = time_sample_on_gpu(torch, eng, E, sts, cpu_sample_indices(sts), ts, dev, args.steps, kw)
+    on_ref_gpu_sample = time_sample_on_gpu(torch, eng, E, sts, cpu_sample_indices(sts, REF_GPU_STRIDE), ts, dev,
+                                           args.steps, kw)
     peak = fp64_peak(torch, None, dev)
+    peak_dmma = fp64_peak(torch, None, dev, "dmma")
     eig_t = statistics.mean(per_call["eigensolve"])
     achieved = flops_eig / eig_t / 1e12
     shares = {k: round(sum(v) / elapsed, 4) for k, v in per_call.items()}
@@ -353,8 +493,9 @@ def run_gpu(args, rank, world):
                      "traffic_note": "DRAM bytes per eigensolver launch (ncu); H(k)+S(k) are "
                                      f"{2 * 16 * plan.hs_total / 1e9:.1f} GB, re-streamed from HBM every column "
                                      "pass because the 760 problems in flight hold more than L2",
-                     "peak_source": "measured in this run: FP64 FMA probe kernel (GB300 FP64 tensor MMA runs at "
-                                    "the same rate, so this is the FP64 roofline)",
+                     "peak_source": "measured in this run: FP64 FMA probe kernel (skn_fp64_probe); the FP64 "
+                                    "tensor instruction (skn_fp64_probe_dmma) is measured beside it",
+                     "fp64_fma_tflops": peak, "fp64_dmma_tflops": peak_dmma,
                      "algorithmic": "32/3 n^3 real flops per complex k-point (zpotrf 4/3 + zhegst 4 + zhetrd 16/3), "
                                     "8/3 n^3 per real one (2k integer: dpotrf + dsygst + dsytrd)",
                      "real_k_points": int(plan.prob_real.sum()),
@@ -367,8 +508,12 @@ def run_gpu(args, rank, world):
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e / args.steps},
         "gpu_launches": launches,
         "clocks": clk.summary(),
+        "value_on_cpu_sample": dict(on_cpu_sample, note="the cpu_baseline / --impl reference sample alone, "
+                                                        "device-resident, same path"),
+        "value_on_reference_gpu_sample": dict(on_ref_gpu_sample, note="the sample of reference_gpu_path alone, "
+                                                                      "device-resident, same path"),
     }
-    return out, sts, tables, sd
+    return out, sts, tables, sd, res
 
 
 def _single_thread_workers():
@@ -393,7 +538,16 @@ def run_training_step(dev, steps=3):
     rec = [T.train_step(model, opt, sts, dos_t, gap_t, sd, dev) for _ in range(steps)]
     solves = sum(len(st["kpoints"]) for st in sts)
     ms = [1e3 * (r["forward_s"] + r["backward_s"]) for r in rec]
+    # the same step on the first three structures alone: the ones the reference's autograd step is timed on
+    few = sts[:3]
+    model3 = M.MultiElementSkfParameterOptimizer.from_tables(tables).to(dev)
+    opt3 = torch.optim.AdamW(model3.parameters(), lr=1e-4)
+    T.train_step(model3, opt3, few, dos_t[:3], gap_t[:3], sd, dev)
+    rec3 = [T.train_step(model3, opt3, few, dos_t[:3], gap_t[:3], sd, dev) for _ in range(steps)]
+    ms3 = statistics.median(1e3 * (r["forward_s"] + r["backward_s"]) for r in rec3)
     return {"structures": len(sts), "k_point_solves": solves, "ms_per_step": statistics.median(ms),
+            "same_structures": {"structures": len(few), "ms_per_step": ms3,
+                                "note": "the first three structures of the batch, as timed for the reference"},
             "forward_ms": 1e3 * statistics.median(r["forward_s"] for r in rec),
             "backward_ms": 1e3 * statistics.median(r["backward_s"] for r in rec),
             "loss_first": rec[0]["loss"], "loss_last": rec[-1]["loss"],
@@ -494,7 +648,10 @@ def run_large_structure(dev):
                     f"{E.cluster_for(n)} CTAs per k-point"}
 
 
-def run_reference_gpu(dev, sts, tables, sd, stride=32, limit=8):
+REF_GPU_STRIDE = 32       # reference GPU path: every 32nd structure by size (8 of the 256)
+
+
+def run_reference_gpu(dev, sts, tables, sd, stride=REF_GPU_STRIDE, limit=8):
     """The plain per-structure GPU path: the reference package itself (installed in baseline/_ref by
     ``pip install --target baseline/_ref <reference>``) with device="cuda", one structure per call, on
     every ``stride``-th structure of the workload by size.  Its optional imports (ase, jarvis,
@@ -523,6 +680,8 @@ def run_reference_gpu(dev, sts, tables, sd, stride=32, limit=8):
     ref = refharness.import_reference()
     model = refharness.build_reference_model(ref, tables)
     sample = cpu_sample(sts, stride)[:limit]
+    for st in sample:
+        st.setdefault("weights", np.full(len(st["kpoints"]), 1.0 / len(st["kpoints"])))
     P = ref.atoms.Periodic
     orig = P._kpoints
     tot_k, tot_t, per = 0, 0.0, []
@@ -607,6 +766,30 @@ def run_reference_gpu_subprocess(args) -> dict:
         return {"reference_gpu_path": {"unavailable": f"worker exited {r.returncode}"}}
 
 
+def north_star_ratios(out: dict) -> dict:
+    """The two speed-up targets against the reference's own code on the same GPU:
+    ``vs_plain_gpu``: k-point solves/s of this path over the reference's per-structure GPU path
+    (target >= 10x), on the full batch and on the reference's sample alone;
+    ``training_vs_reference_autograd``: the reference's autograd training time over this path's
+    adjoint training step, per structure (target >= 5x)."""
+    r = {}
+    ref = out.get("reference_gpu_path") or {}
+    if ref.get("value"):
+        same = (out.get("value_on_reference_gpu_sample") or {}).get("value")
+        r["vs_plain_gpu"] = {"full_batch": out["value"] / ref["value"],
+                             "same_sample": (same / ref["value"]) if same else None,
+                             "e2e_full_batch": out["e2e"]["value"] / ref["value"], "target": 10.0}
+    tr = out.get("reference_gpu_training") or {}
+    ts_ = out.get("training_step") or {}
+    if tr.get("seconds_per_structure") and ts_.get("ms_per_step"):
+        ours = ts_["ms_per_step"] * 1e-3 / ts_["structures"]
+        same = (ts_.get("same_structures") or {}).get("ms_per_step")
+        r["training_vs_reference_autograd"] = {
+            "per_structure": tr["seconds_per_structure"] / ours,
+            "same_structures": (tr["seconds"] / (same * 1e-3)) if same else None, "target": 5.0}
+    return r
+
+
 def reference_gpu_worker(args):
     import contextlib
     import torch
@@ -618,48 +801,59 @@ def reference_gpu_worker(args):
     print(json.dumps({"reference_gpu_path": a, "reference_gpu_training": b}))
 
 
-def run_cpu_baseline(sts, tables, sd, reps=1):
-    _single_thread_workers()
-    sample = cpu_sample(sts)
-    sub = sub_tables_for(sample, tables)
+def run_cpu_baseline(args, gpu_res=None, reps=1):
+    """The oracle on the host cores over the stratified sample (one pass), plus, when the GPU arm's
+    last timed step is given, the parity of that step against the oracle's results."""
+    from slakonet_gb300 import engine as E
+    sts, tables, sd = workload(args.structures, args.seed)
+    for st in sts:
+        st["weights"] = np.full(len(st["kpoints"]), 1.0 / len(st["kpoints"]))
+    idx = cpu_sample_indices(sts)
     cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores, initializer=_pool_init) as pool:
-        best = None
+    with oracle_pool(args.structures, args.seed, cores) as pool:
+        best, res = None, None
         for _ in range(reps):
-            solves, sec = time_oracle(sample, sub, sd, pool, cores)
+            solves, sec, props = time_oracle(sts, idx, tables, sd, pool)
             v = solves / sec
-            best = v if best is None else max(best, v)
-    return {"value": best, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"every {ordinal(SAMPLE_STRIDE)} structure by size ({len(sample)} structures, {solves} k-point "
-                      f"solves, {sec:.1f} s), numpy/LAPACK oracle, one process per core"}
+            if best is None or v > best:
+                best, res = v, (solves, sec, props)
+    solves, sec, props = res
+    out = {"value": best, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"every {ordinal(SAMPLE_STRIDE)} structure by size ({len(idx)} structures, {solves} k-point "
+                     f"solves, {sec:.1f} s); numpy/LAPACK oracle on {cores} one-thread processes: real-space blocks once per "
+                     f"structure, then (structure, {K_CHUNK}-k-point chunk) Bloch sums and eigensolves, largest first; "
+                     "then Fermi level, gap and DOS per structure"}
+    parity = parity_against_oracle(gpu_res, idx, props, E.STAT) if gpu_res is not None else None
+    return out, parity
 
 
 def run_reference(args):
-    """CPU oracle arm: bounded stratified sample, all host cores, K timed steps after W warm-ups."""
+    """Reference arm: the reference path is Python, so its CPU implementation is the oracle port, run on the
+    same stratified sample as the GPU arm's cpu_baseline with every host core, K timed steps after W
+    warm-ups (one warm-up pass is enough to load every worker)."""
     sts, tables, sd = workload(args.structures, args.seed)
-    _single_thread_workers()
-    sample = cpu_sample(sts, SAMPLE_STRIDE * 2)
-    sub = sub_tables_for(sample, tables)
+    idx = cpu_sample_indices(sts)
     cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores, initializer=_pool_init) as pool:
+    with oracle_pool(args.structures, args.seed, cores) as pool:
         for _ in range(min(args.warmup, 1)):
-            time_oracle(sample[:4], sub, sd, pool, cores)
+            time_oracle(sts, idx[-4:], tables, sd, pool)
         tot_s, tot_t = 0, 0.0
         for _ in range(args.steps):
-            s, t = time_oracle(sample, sub, sd, pool, cores)
-            tot_s += s
-            tot_t += t
+            s_, t_, _ = time_oracle(sts, idx, tables, sd, pool)
+            tot_s += s_
+            tot_t += t_
     v = tot_s / tot_t
+    sample = (f"every {ordinal(SAMPLE_STRIDE)} structure by size ({len(idx)} structures, {tot_s // max(args.steps, 1)} "
+              f"k-point solves per step); numpy/LAPACK oracle on {cores} one-thread processes: real-space blocks once "
+              f"per structure, then (structure, {K_CHUNK}-k-point chunk) Bloch sums and eigensolves, largest first; "
+              "then Fermi level, gap and DOS per structure")
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD, "structures": args.structures, "seed": args.seed,
-                       "sample_structures": len(sample)},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"every {ordinal(2 * SAMPLE_STRIDE)} structure by size ({len(sample)} structures,"
-                                       f" {tot_s // max(args.steps, 1)} k-point solves per step)"},
+                       "sample_structures": len(idx), "same_sample_as": "cpu_baseline and value_on_cpu_sample of "
+                                                                        "the GPU arm"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -682,8 +876,9 @@ def main():
     ap.add_argument("--no-serving-capacity", action="store_true", help="skip the all-at-once capacity leg")
     ap.add_argument("--serving-only", action="store_true",
                     help="run only the serving measurement (one GPU) and print its JSON line with clocks")
-    ap.add_argument("--reference-gpu", action="store_true",
-                    help="also time the reference package (baseline/_ref) per structure on the GPU, on a sample")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference package (baseline/_ref) per structure on the GPU, and its "
+                         "autograd training step")
     ap.add_argument("--reference-gpu-worker", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--large-structure", action="store_true",
                     help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
@@ -711,7 +906,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     r = run_gpu(args, rank, world)
     if rank == 0:
-        out, sts, tables, sd = r
+        out, sts, tables, sd, gpu_res = r
         if world == 1 and not args.no_extras:
             import torch
             dev = torch.device("cuda", 0)
@@ -724,12 +919,13 @@ def main():
             import torch
             log("large structure")
             out["large_structure"] = run_large_structure(torch.device("cuda", 0))
-        if world == 1 and args.reference_gpu:
+        if world == 1 and not args.no_reference_gpu:
             log("reference per-structure GPU path and training step (subprocess)")
             out.update(run_reference_gpu_subprocess(args))
+            out.update(north_star_ratios(out))
         if world == 1 and not args.no_cpu_baseline:
-            log("cpu baseline")
-            out["cpu_baseline"] = run_cpu_baseline(sts, tables, sd)
+            log("cpu baseline and parity of the timed step")
+            out["cpu_baseline"], out["parity"] = run_cpu_baseline(args, gpu_res)
         log("done")
         print(json.dumps(out))
     if world > 1:

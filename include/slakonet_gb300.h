@@ -191,17 +191,24 @@ int skn_eigh_vectors_scratch_bytes(int n_prob, int max_n, int64_t* bytes);
  * service that keeps cudaMalloc/cudaFree (which can synchronise the device or
  * fail under memory pressure) out of its request path.
  * Same outputs, same contract, minus tri, scratch and work_counter: those live
- * in one fixed library-owned device array (about 40 MiB per device, reserved
- * when the library's module is loaded on that device).
+ * in one fixed library-owned device array (about 40 MiB per device), held by
+ * every device that loads the library until the process exits.
  *   n_rows   length of eig = sum of n[p] (every eig_off[p] + n[p] <= n_rows)
  * Limits: max_n <= SKN_NOALLOC_MAX_N and n_rows <= SKN_NOALLOC_MAX_ROWS, else
- * SKN_ERR_CAPACITY and nothing is launched.  The vector stage runs on as many
- * CTAs as the fixed workspace holds (up to 2 per SM), so large batches are
- * slower than with skn_eigh_gen_vectors.
- * The first call on a device looks up the array's address on the current
- * device; make it before any stream capture.  Calls share the array: two
- * calls in flight at once on one device (other streams or host threads) race
- * and corrupt each other; order them on one stream or serialise them.
+ * SKN_ERR_CAPACITY and nothing is launched.  On the device, a problem with
+ * n[p] > max_n or eig_off[p] + n[p] > n_rows is skipped with status[p] =
+ * SKN_ERR_CAPACITY and its outputs untouched, so an understated n_rows cannot
+ * write past the fixed array.  The vector stage runs on as many CTAs as the
+ * fixed workspace holds (up to 2 per SM), so large batches are slower than
+ * with skn_eigh_gen_vectors.
+ * The array is set aside when the library's CUDA module is loaded on a device;
+ * with lazy module loading (the CUDA default) that is the first call on that
+ * device, so make one call at start-up (n_prob = 0 is enough), before any
+ * stream capture.  Every call looks up the array's device address on the
+ * current device.  Calls share the array, which keeps the last call's
+ * contents: two calls in flight at once on one device (other streams or host
+ * threads) race and corrupt each other; order them on one stream or serialise
+ * them.
  */
 #define SKN_NOALLOC_MAX_N 512
 #define SKN_NOALLOC_MAX_ROWS 262144             /* 8 MiB of tridiagonal rows            */
@@ -368,6 +375,16 @@ int skn_dos_backward(int n_struct, const int64_t* eig_off, const int32_t* nk, co
  * measure the FP64 roofline the eigensolver is bound by.
  */
 int skn_fp64_probe(double* out, int blocks, int iters, cudaStream_t stream);
+
+/*
+ * The same measurement on the FP64 tensor instruction (mma.sync m8n8k4 f64):
+ * `blocks` CTAs of 256 threads, each warp running 8 independent chains of
+ * `iters` instructions (512 flops each per warp), `out` holds blocks*256
+ * doubles.  No reference counterpart: it shows whether FP64 tensor MMA is
+ * faster than FP64 FMA on this GPU, which decides how the eigensolver's
+ * updates are shaped.
+ */
+int skn_fp64_probe_dmma(double* out, int blocks, int iters, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -347,24 +347,28 @@ def onsite_vector(numbers: Sequence[int], tables: dict, shell_dict, kind: str = 
     return np.array(out, dtype=np.float64)
 
 
-def hk_sk(structure: dict, tables: dict, shell_dict, kpoints: np.ndarray, cutoff: float = 10.0):
+def hk_sk(structure: dict, tables: dict, shell_dict, kpoints: np.ndarray, cutoff: float = 10.0, blocks=None):
     """``H(k), S(k)`` as ``[nk, n, n]`` complex128.
 
     ``M(k) = diag(onsite) + sum_bonds block * exp(i 2 pi k . T)``: the Bloch
     sum of ``_pe_sk_data2`` (slakonet/slaterkoster.py:971-1010) with the
-    phase of ``Periodic.phase`` (slakonet/atoms.py:543-558).
+    phase of ``Periodic.phase`` (slakonet/atoms.py:543-558).  ``blocks``, when
+    given, is ``(real_space_blocks(.., "H"), real_space_blocks(.., "S"))`` of
+    this structure, which do not depend on k (the reference also builds them
+    once per structure).
     """
     numbers = [int(z) for z in structure["numbers"]]
     atom_off, _, n = orbital_layout(numbers, shell_dict)
     kpoints = np.asarray(kpoints, dtype=np.float64).reshape(-1, 3)
     res = []
-    for kind in ("H", "S"):
-        i, j, T, blocks = real_space_blocks(structure, tables, shell_dict, cutoff, kind)
+    for q, kind in enumerate(("H", "S")):
+        i, j, T, blocks_k = (blocks[q] if blocks is not None
+                             else real_space_blocks(structure, tables, shell_dict, cutoff, kind))
         M = np.zeros((len(kpoints), n, n), dtype=np.complex128)
         if len(i):
             ph = np.exp(1j * (2.0 * np.pi * kpoints) @ T.T.astype(np.float64))   # [nk, nb]
             for b, (a1, a2) in enumerate(zip(i, j)):
-                blk = blocks[b]
+                blk = blocks_k[b]
                 o1, o2 = atom_off[a1], atom_off[a2]
                 M[:, o1:o1 + blk.shape[0], o2:o2 + blk.shape[1]] += ph[:, b, None, None] * blk[None]
         idx = np.arange(n)

@@ -45,6 +45,7 @@ SIGNATURES = {
     "skn_fermi_gap": [I32, P, P, P, P, P, P, P, F64, F64, I32, P, P, P, P],
     "skn_dos": [I32, P, P, P, P, P, P, P, F64, F64, I32, F64, F64, P, P, P, P],
     "skn_fp64_probe": [P, I32, I32, P],
+    "skn_fp64_probe_dmma": [P, I32, I32, P],
     "skn_eigh_gen_vectors": [I32, P, P, P, P, P, P, P, P, P, P, P, I64, P, I32, P],
     "skn_eigh_vectors_scratch_bytes": [I32, I32, P],
     "skn_eigh_gen_vectors_noalloc": [I32, P, P, P, P, P, P, P, P, P, I64, I32, P],
@@ -56,7 +57,7 @@ SIGNATURES = {
     "skn_dos_backward": [I32, P, P, P, P, P, P, P, F64, F64, I32, F64, F64, P, P, I32, P],
     "skn_atom_pdos": [I32, I32, I32, P, P, P, I32, F64, F64, F64, I32, F64, F64, P, P, P, P],
 }
-for _sfx in ("_t64", "_t256"):
+for _sfx in ("_t64", "_t256", "_blk", "_blk256"):
     SIGNATURES["skn_eigh_gen_batched" + _sfx] = SIGNATURES["skn_eigh_gen_batched"]
     SIGNATURES["skn_eigh_gen_batched_real" + _sfx] = SIGNATURES["skn_eigh_gen_batched"]
     SIGNATURES["skn_eigh_gen_vectors" + _sfx] = SIGNATURES["skn_eigh_gen_vectors"]
