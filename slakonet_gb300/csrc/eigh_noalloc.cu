@@ -5,14 +5,16 @@
 // the default 128-thread launch shape).  Their scratch -- the two queue
 // counters, the tridiagonal/tau rows and the inverse-iteration workspace --
 // lives in one file-scope __device__ array of fixed size instead of buffers
-// the caller passes.  The array is reserved when the CUDA module holding this
-// file is loaded, once per device, and its device address is looked up once
-// per device on the first call.
+// the caller passes.  The array is set aside when the CUDA module holding this
+// file is loaded on a device; with lazy module loading (the CUDA runtime's
+// default) that happens inside the first call on that device, which is why
+// callers make one call (n_prob = 0 is enough) at start-up.  Every call looks
+// up the array's device address on the current device: the lookup is cheap
+// once the module is loaded, and an address kept from an earlier context
+// would be stale after cudaDeviceReset.
 #define SKN_EIG_KERNELS_ONLY
 #define SKN_EIG_NS_TAG _noalloc
 #include "eigh.cu"
-
-#include <mutex>
 
 namespace {
 
@@ -27,24 +29,13 @@ static_assert((int64_t)5 * SKN_NOALLOC_MAX_N * VNT <= NA_SCRATCH_DOUBLES, "one v
 // [counters | tri: 4 doubles per eigenvalue row | inverse-iteration scratch]
 static __device__ __align__(256) double g_noalloc[NA_TOTAL_DOUBLES];
 
-constexpr int NA_MAX_DEVICES = 64;
-std::mutex g_noalloc_mu;
-double* g_noalloc_addr[NA_MAX_DEVICES] = {};
-
-// Device address of g_noalloc on the current device (looked up once per device).
+// Device address of g_noalloc on the current device.  In host code the name g_noalloc is a host-side
+// stand-in, not a device address, so kernels get only what this lookup returns.
 cudaError_t noalloc_base(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= NA_MAX_DEVICES) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (g_noalloc_addr[dev] == nullptr) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc);
-    if (e != cudaSuccess) return e;
-    g_noalloc_addr[dev] = static_cast<double*>(p);
-  }
-  *out = g_noalloc_addr[dev];
+  *out = static_cast<double*>(p);
   return cudaSuccess;
 }
 
@@ -55,11 +46,12 @@ extern "C" int skn_eigh_gen_vectors_noalloc(int n_prob, const int32_t* n, const 
                                             double* eig, double* vec, int32_t* status, int64_t n_rows, int max_n,
                                             cudaStream_t stream) {
   if (n_prob < 0 || max_n < 0 || n_rows < 0) return SKN_ERR_ARG;
+  // the lookup comes first so that a call with no problems loads the module on this device (a warm-up)
+  double* base = nullptr;
+  if (noalloc_base(&base) != cudaSuccess) return SKN_ERR_CUDA;
   if (n_prob == 0) return SKN_OK;
   if (!n || !hs_off || !eig_off || !order || !H || !S || !eig || !vec || !status) return SKN_ERR_ARG;
   if (max_n > SKN_NOALLOC_MAX_N || n_rows > SKN_NOALLOC_MAX_ROWS) return SKN_ERR_CAPACITY;
-  double* base = nullptr;
-  if (noalloc_base(&base) != cudaSuccess) return SKN_ERR_CUDA;
   int32_t* counter = reinterpret_cast<int32_t*>(base);
   double* tri = base + NA_COUNTER_DOUBLES;
   double* scratch = tri + NA_TRI_DOUBLES;
@@ -83,7 +75,7 @@ extern "C" int skn_eigh_gen_vectors_noalloc(int n_prob, const int32_t* n, const 
   // only the queue counters must start at zero; every tri row and scratch entry is written before it is read
   if (cudaMemsetAsync(counter, 0, 2 * sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
   k_eigh_gen<false><<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
-                                         counter, mn, use_smem_mats, tri);
+                                         counter, mn, use_smem_mats, tri, n_rows);
   if (cudaPeekAtLastError() != cudaSuccess) return SKN_ERR_CUDA;
   k_eigvec<<<vgrid, VNT, vec_smem_bytes(mn), stream>>>(n_prob, n, hs_off, eig_off, order, (const double2*)H,
                                                        (const double2*)S, eig, tri, status, (double2*)vec, scratch,

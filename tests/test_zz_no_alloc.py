@@ -114,3 +114,48 @@ def test_noalloc_refuses_sizes_above_its_limits():
     torch.cuda.synchronize(DEV)
     # nothing ran
     assert bool((eig == -7.0).all()) and bool((st_ == -1).all()) and torch.equal(H, hs.H)
+
+
+def test_noalloc_zero_problem_call_is_a_warm_up():
+    """A call with no problems loads the module and looks up the fixed array, and launches nothing."""
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(DEV).cuda_stream
+    assert lib.skn_eigh_gen_vectors_noalloc(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, stream) == _lib.SKN_OK
+
+
+def test_noalloc_skips_problems_past_an_understated_row_count():
+    """n_rows one short of the batch's eigenvalue rows: the problem whose rows end past it is skipped on the
+    device with SKN_ERR_CAPACITY and its outputs untouched; every other problem matches the allocating entry."""
+    g = golden("rand_b")
+    st, tables, sd = load_case(g)
+    plan, db, hs = _batch([dict(st, kpoints=g["kpoints"][:6])], tables, sd)
+    n_prob = len(plan.prob_n)
+    eig_a, vec_a, st_a = _allocating(plan, db, hs.H, hs.S)
+    H, S = hs.H.clone(), hs.S.clone()
+    eig = torch.full((plan.eig_total,), -7.0, dtype=torch.float64, device=DEV)
+    vec = torch.full_like(H, -3.0)
+    st_ = torch.full((n_prob,), -1, dtype=torch.int32, device=DEV)
+    stream = torch.cuda.current_stream(DEV).cuda_stream
+    lib = _lib.load()
+    rc = lib.skn_eigh_gen_vectors_noalloc(n_prob, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(db.order), ptr(H),
+                                          ptr(S), ptr(eig), ptr(vec), ptr(st_), plan.eig_total - 1, plan.max_n,
+                                          stream)
+    torch.cuda.synchronize(DEV)
+    assert rc == _lib.SKN_OK
+    eoff = db.eoff.cpu().tolist()
+    hoff = db.hs_off.cpu().tolist()
+    nv = db.n.cpu().tolist()
+    status = st_.cpu().tolist()
+    over = [p for p in range(n_prob) if eoff[p] + nv[p] > plan.eig_total - 1]
+    assert len(over) == 1
+    for p in range(n_prob):
+        n = nv[p]
+        e = slice(eoff[p], eoff[p] + n)
+        v = slice(2 * hoff[p], 2 * (hoff[p] + n * n))    # H is held as doubles: 2 per complex entry
+        if p in over:
+            assert status[p] == _lib.SKN_ERR_CAPACITY
+            assert bool((eig[e] == -7.0).all()) and bool((vec[v] == -3.0).all())
+        else:
+            assert status[p] == _lib.SKN_OK
+            assert float((eig[e] - eig_a[e]).abs().max()) * EV <= 1e-8
+            assert float((vec[v] - vec_a[v]).abs().max()) <= 1e-10
