@@ -1,8 +1,9 @@
 """Generate the golden fixtures by running the reference SlakoNet code.
 
-Run in a container that has the reference at ``/root/reference``:
+Run in a container that has the reference source, with ``SLAKONET_REF`` naming the
+directory that holds its ``slakonet`` package:
 
-    python tests/golden/make_golden.py
+    SLAKONET_REF=<reference checkout> python tests/golden/make_golden.py
 
 Every fixture is produced by the reference's own functions on seeded
 synthetic inputs from ``slakonet_gb300.synthetic``; the numbers are frozen
@@ -331,6 +332,111 @@ def fixture_gradients():
             print("  ", f[0], f[1], f"{f[2]: .6e} {f[3]: .6e} {f[4]: .6e}")
 
 
+TRAIN_LR = 1e-3
+TRAIN_STEPS = 3
+
+
+def _train_structures(seed):
+    """Two small C/Si cells with Gamma-centred 3x3x2 grids (complex k-points among them)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for numbers in ([6, 14, 14], [14, 6, 6, 14]):
+        st = syn.random_structure(rng, len(numbers), zmax=14)
+        st["numbers"] = np.array(numbers)
+        st["kpoints"] = syn.gamma_centred_kpoints((3, 3, 2))
+        out.append(st)
+    return out
+
+
+def _train_forward(model, st, sd):
+    """The reference's properties call with gradients, then the 1000-point DOS on [-20, 10] eV of the
+    fitting workload from its own calculate_dos (slakonet/main.py:709-797)."""
+    try:
+        with inject_kpoints(st["kpoints"]):
+            props, ok = model.compute_multi_element_properties(geometry=geometry(st), shell_dict=sd, device="cpu",
+                                                               get_fermi=True)
+    except IndexError:          # every k-point dropped: the reference packs an empty list
+        raise ValueError("the reference dropped every k-point (S(k) not positive definite)")
+    if props["eigenvalues"].shape[1] != len(st["kpoints"]):
+        raise ValueError("the reference dropped k-points whose S(k) is not positive definite")
+    _, dos = props["calc"].calculate_dos(energy_range=(-20.0, 10.0), num_points=1000, sigma=0.1)
+    return dos, props["band_gap_eV"]
+
+
+def fixture_training():
+    """The first structure seed (from 77) whose two cells keep every S(k) positive definite over the three
+    steps (apply_constraints rescales negative and small overlap entries, which can break definiteness)."""
+    for seed in range(77, 120):
+        try:
+            return _fixture_training(seed)
+        except ValueError as e:
+            print(f"structure seed {seed}: {e}")
+    raise RuntimeError("no structure seed kept S(k) positive definite")
+
+
+def _fixture_training(struct_seed):
+    """Three steps of the reference's fitting loop (slakonet/optim.py:1656-1772) on two structures:
+    apply_constraints, per-structure loss weighted by atom count, 1e-10 * sum(theta^2), backward with the
+    eigenvector conjugate restored in _SymEigB.backward, gradient clipping at 2.0, AdamW, ReduceLROnPlateau.
+    The per-structure loss is the fitting workload's DOS MSE plus band-gap absolute error, against targets
+    from the same reference call on tables with 5 % perturbed amplitudes (seed 1)."""
+    sd_all = syn.default_shell_dict()
+    sd = {6: sd_all[6], 14: sd_all[14]}
+    tables = syn.make_tables([6, 14], sd, seed=4)
+    sts = _train_structures(struct_seed)
+    target_model = build_reference_model(ref, syn.perturb_tables(tables, 0.05, 1))
+    dos_t, gap_t = [], []
+    with torch.no_grad():
+        for st in sts:
+            d, g = _train_forward(target_model, st, sd)
+            dos_t.append(d.clone())
+            gap_t.append(float(g))
+    model = build_reference_model(ref, tables)
+    opt = torch.optim.AdamW(model.parameters(), lr=TRAIN_LR)
+    sched = torch.optim.lr_scheduler.ReduceLROnPlateau(opt, mode="min", factor=0.8, patience=10)
+    keys = [(pk, kind, lk) for pk, o in model.skf_optimizers.items() for kind, pd in (("h", o.h_params),
+                                                                                      ("s", o.s_params))
+            for lk in pd]
+    payload = {"tables_checksum": tables_checksum(tables), "table_seed": 4, "lr": TRAIN_LR,
+               "struct_seed": struct_seed,
+               "dos_target": np.stack([d.numpy() for d in dos_t]), "gap_target": np.array(gap_t),
+               "param_keys": np.array(["|".join(k) for k in keys])}
+    for i, st in enumerate(sts):
+        for f in ("numbers", "positions", "cell", "kpoints"):
+            payload[f"s{i}_{f}"] = np.asarray(st[f])
+    orig = ref.utils._SymEigB.backward
+    ref.utils._SymEigB.backward = staticmethod(_fixed_symeig_backward)
+    try:
+        for step in range(TRAIN_STEPS):
+            opt.zero_grad()
+            model.apply_constraints()
+            losses, wsum = [], 0.0
+            for st, d_t, g_t in zip(sts, dos_t, gap_t):
+                dos, gap = _train_forward(model, st, sd)
+                loss = torch.mean((dos - d_t) ** 2) + torch.abs(gap - g_t)
+                w = float(len(st["numbers"]))
+                losses.append(loss * w)
+                wsum += w
+            batch = sum(losses) / wsum
+            reg = 1e-10 * sum(torch.sum(p ** 2) for p in model.parameters())
+            total = batch + reg
+            total.backward()
+            torch.nn.utils.clip_grad_norm_(model.parameters(), max_norm=2.0)
+            for (pk, kind, lk) in keys:             # the clipped gradient this step's AdamW update uses
+                prm = getattr(model.skf_optimizers[pk], f"{kind}_params")[lk]
+                payload[f"grad{step}|{pk}|{kind}|{lk}"] = prm.grad.detach().numpy().copy()
+            opt.step()
+            sched.step(total)
+            payload[f"loss_{step}"] = float(total.detach())
+            for (pk, kind, lk) in keys:
+                prm = getattr(model.skf_optimizers[pk], f"{kind}_params")[lk]
+                payload[f"step{step}|{pk}|{kind}|{lk}"] = prm.detach().numpy().copy()
+            print(f"training step {step}: loss {float(total):.12e}")
+    finally:
+        ref.utils._SymEigB.backward = orig
+    np.savez_compressed(os.path.join(HERE, "train_steps.npz"), **payload)
+
+
 def fixture_energy_forces(name, st, shell_dict, table_seed, mesh):
     """get_energy / get_forces of compute_multi_element_properties (slakonet/optim.py:1066-1071):
     Fermi-smeared band energy (slakonet/main.py:1430-1448) and central-difference forces on the
@@ -384,6 +490,9 @@ if __name__ == "__main__":
     if "--pdos-only" in sys.argv:
         fixtures_pdos()
         sys.exit(0)
+    if "--training-only" in sys.argv:
+        fixture_training()
+        sys.exit(0)
     if "--energy-forces-only" in sys.argv:
         fixtures_energy_forces()
         sys.exit(0)
@@ -399,4 +508,5 @@ if __name__ == "__main__":
     fixture_gradients()
     fixtures_pdos()
     fixtures_energy_forces()
+    fixture_training()
     print("golden fixtures written to", HERE)

@@ -1,7 +1,8 @@
 """Import harness for the reference SlakoNet package (fixture generation only).
 
 This module is used by ``make_golden.py`` in a container that holds a
-read-only copy of the reference at ``/root/reference``.  The library and the
+checkout of the reference; ``SLAKONET_REF`` names its directory (the one that
+contains the ``slakonet`` package).  The library and the
 GPU tests never import it: the reference source tree does not exist on the
 GPU hosts, and the committed golden fixtures are what travels.  The one other
 user is ``bench.py --reference-gpu``, which points ``REF_ROOT`` at a pip
@@ -16,10 +17,14 @@ needs from them is ``jarvis.core.specie.atomic_numbers_to_symbols``, used by
 the model's atomic-number -> symbol map (slakonet/optim.py:162-164); the
 stand-in maps through the reference's own ``slakonet.elements`` table.
 """
+import os
 import sys
 import types
 
-REF_ROOT = "/root/reference"
+# Directory holding the reference's ``slakonet`` package: $SLAKONET_REF, else the pip installation
+# of the reference in baseline/_ref beside this repository's root.
+REF_ROOT = os.environ.get("SLAKONET_REF") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "baseline", "_ref")
 
 
 def _install_stubs():

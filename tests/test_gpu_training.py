@@ -1,0 +1,86 @@
+"""The fitting step on the GPU against the reference's own training loop (needs a GB300).
+
+``train_steps.npz`` holds three steps of the reference's fitting loop
+(slakonet/optim.py:1656-1772), run by the reference itself with its
+eigenvector conjugate restored: apply_constraints, per-structure loss
+(1000-point DOS MSE plus band-gap absolute error) weighted by atom count,
+1e-10 * sum(theta^2), backward, clipping at 2.0, AdamW (lr 1e-3) and
+ReduceLROnPlateau, on two C/Si cells with Gamma-centred 3x3x2 grids.
+``training.train_step`` runs the same three steps with the hand-written
+adjoint.  After every step:
+- the loss equals the reference's within 1e-10 relative;
+- the clipped gradient of every parameter tensor equals the reference's within
+  1e-9 of the step's largest gradient entry;
+- every parameter whose gradient has reached 1e-6 (100 x AdamW's eps) in some
+  step so far equals the reference's within 1e-10 of its tensor's largest
+  entry.  Below that, AdamW's update lr * g / (|g| + eps) turns the rounding
+  of a near-zero gradient into an O(lr) change, so those entries are held to
+  1e-3 * lr absolute instead.
+"""
+import numpy as np
+import pytest
+import torch
+
+from _cases import tables_checksum
+from conftest import golden
+from slakonet_gb300 import model as M, synthetic as syn, training as T
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+REL = 1e-10
+
+
+def _setup():
+    g = golden("train_steps")
+    sd_all = syn.default_shell_dict()
+    sd = {6: sd_all[6], 14: sd_all[14]}
+    tables = syn.make_tables([6, 14], sd, seed=int(g["table_seed"]))
+    np.testing.assert_allclose(tables_checksum(tables), g["tables_checksum"], rtol=1e-12, atol=1e-300)
+    sts = []
+    for i in range(2):
+        k = g[f"s{i}_kpoints"]
+        sts.append({"numbers": g[f"s{i}_numbers"], "positions": g[f"s{i}_positions"], "cell": g[f"s{i}_cell"],
+                    "kpoints": k, "weights": np.full(len(k), 1.0 / len(k))})
+    return g, sd, tables, sts
+
+
+def test_train_steps_follow_the_reference_loop():
+    g, sd, tables, sts = _setup()
+    model = M.MultiElementSkfParameterOptimizer.from_tables(tables).to(DEV)
+    opt = torch.optim.AdamW(model.parameters(), lr=float(g["lr"]))
+    sched = torch.optim.lr_scheduler.ReduceLROnPlateau(opt, mode="min", factor=0.8, patience=10)
+    dos_t = torch.tensor(g["dos_target"], device=DEV)
+    gap_t = torch.tensor(g["gap_target"], device=DEV)
+    lr = float(g["lr"])
+    keys = [str(k) for k in g["param_keys"]]
+    gmax_seen = {k: np.zeros_like(g[f"grad0|{k}"]) for k in keys}
+    for step in range(3):
+        r = T.train_step(model, opt, sts, dos_t, gap_t, sd, DEV, scheduler=sched)
+        ref_loss = float(g[f"loss_{step}"])
+        dl = abs(r["loss"] - ref_loss) / abs(ref_loss)
+        gscale = max(float(np.abs(g[f"grad{step}|{k}"]).max()) for k in keys)
+        worst_g = worst_p = worst_small = 0.0
+        n_small = 0
+        for key in keys:
+            pk, kind, lk = key.split("|")
+            prm = getattr(model.skf_optimizers[pk], f"{kind}_params")[lk]
+            g_ref = g[f"grad{step}|{key}"]
+            worst_g = max(worst_g, float(np.abs(prm.grad.detach().cpu().numpy() - g_ref).max()) / gscale)
+            gmax_seen[key] = np.maximum(gmax_seen[key], np.abs(g_ref))
+            ours = prm.detach().cpu().numpy()
+            ref = g[f"step{step}|{key}"]
+            diff = np.abs(ours - ref)
+            big = gmax_seen[key] >= 1e-6
+            if big.any():
+                worst_p = max(worst_p, float(diff[big].max()) / max(float(np.abs(ref).max()), 1e-300))
+            if (~big).any():
+                worst_small = max(worst_small, float(diff[~big].max()))
+                n_small += int((~big).sum())
+        print(f"step {step}: loss {r['loss']:.15e} (reference {ref_loss:.15e}, rel {dl:.1e}); gradients max "
+              f"{worst_g:.1e} of the largest; parameters max rel {worst_p:.1e}; {n_small} entries with "
+              f"|g| < 1e-6 within {worst_small:.1e} (lr {lr:g}); structures used {r['structures_used']}")
+        assert r["structures_used"] == 2
+        assert dl <= REL
+        assert worst_g <= 1e-9
+        assert worst_p <= REL
+        assert worst_small <= 1e-3 * lr
