@@ -22,8 +22,10 @@ LIB = os.path.join(PKG, "libslakonet_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # Extra launch shapes of the eigensolver, exported with a suffix and chosen per problem-size
-# bucket by slakonet_gb300.autotune: (suffix, threads per CTA, CTAs per SM, unroll, shared-memory staging n).
-EIG_SHAPES = [("_t64", 64, 8, 2, 16), ("_t256", 256, 3, 2, 32)]
+# bucket by slakonet_gb300.autotune: (suffix, threads per CTA, CTAs per SM, unroll, shared-memory staging n,
+# blocked Cholesky and reduction).
+EIG_SHAPES = [("_t64", 64, 8, 2, 16, 0), ("_t256", 256, 3, 2, 32, 0), ("_blk", 128, 3, 2, 24, 1),
+              ("_blk256", 256, 2, 2, 24, 1)]
 
 
 def nvcc() -> str:
@@ -76,9 +78,10 @@ def _build_locked(verbose: bool) -> str:
 
     jobs = [(src, [], "") for src in sources()]
     eig = os.path.join(CSRC, "eigh.cu")
-    for suffix, nt, minb, unr, smem_n in EIG_SHAPES:
+    for suffix, nt, minb, unr, smem_n, blocked in EIG_SHAPES:
         jobs.append((eig, [f"-DSKN_EIG_SUFFIX={suffix}", f"-DSKN_EIG_NT={nt}", f"-DSKN_EIG_MINB={minb}",
-                           f"-DSKN_EIG_UNR={unr}", f"-DSKN_EIG_SMEM_N={smem_n}"], suffix))
+                           f"-DSKN_EIG_UNR={unr}", f"-DSKN_EIG_SMEM_N={smem_n}", f"-DSKN_EIG_BLOCKED={blocked}"],
+                     suffix))
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
         objs = list(ex.map(compile_one, jobs))
     tmp = LIB + ".tmp"

@@ -379,6 +379,242 @@ __device__ void hegs2_lower(double2* __restrict__ A, int lda, const double2* __r
   }
 }
 
+// ------------------------------------- blocked Cholesky and reduction (NB-column panels)
+// The same factorisations in LAPACK's blocked order (zpotrf right-looking, zhegst itype 1,
+// lower).  Per panel: a small unblocked step on the NB x NB diagonal block in shared memory,
+// row-parallel triangular solves of the panel, then one trailing update of the packed lower
+// triangle in which every element accumulates all NB panel terms in registers -- one
+// read-modify-write per element per panel instead of per column, full warps on contiguous
+// elements, and one barrier per phase instead of several per column.
+#ifndef SKN_EIG_BLOCKED
+#define SKN_EIG_BLOCKED 0
+#endif
+constexpr int NB = 32;          // panel width
+constexpr int LDT = NB + 1;     // leading dimension of the shared-memory tiles
+static_assert(SMEM_REGION >= NB * LDT, "the staging region doubles as the first panel tile");
+
+// c - sum_k P[i,k] conj(Q[j,k]) over the NB columns of two panels (column strides lp, lq), two chains.
+template <bool R>
+SKN_DEVINL double2 panel_dot_conj(const double2* __restrict__ Pi, int lp, const double2* __restrict__ Qj, int lq,
+                                  double2 c) {
+  double2 acc1 = make_double2(0.0, 0.0);
+#pragma unroll 8
+  for (int k = 0; k < NB; k += 2) {
+    c = z_fms_conj<R>(z_ld<R>(Pi + (int64_t)k * lp), z_ld<R>(Qj + (int64_t)k * lq), c);
+    acc1 = z_fms_conj<R>(z_ld<R>(Pi + (int64_t)(k + 1) * lp), z_ld<R>(Qj + (int64_t)(k + 1) * lq), acc1);
+  }
+  return make_double2(c.x + acc1.x, c.y + acc1.y);
+}
+
+// x L^H = a for the w entries of one row (stride ld), L lower w x w in the shared tile Lt,
+// rd[j] = 1 / L_jj; in place.  Entries already solved are re-read from memory (same thread).
+template <bool R>
+SKN_DEVINL void row_solve_lh(double2* __restrict__ row, int64_t ld, const double2* __restrict__ Lt, int w,
+                             const double* __restrict__ rd) {
+  for (int j = 0; j < w; ++j) {
+    double2 a0 = z_ld<R>(row + j * ld), a1 = make_double2(0.0, 0.0);
+    int k = 0;
+    for (; k + 1 < j; k += 2) {
+      a0 = z_fms_conj<R>(z_ld<R>(row + k * ld), Lt[j + k * LDT], a0);
+      a1 = z_fms_conj<R>(z_ld<R>(row + (k + 1) * ld), Lt[j + (k + 1) * LDT], a1);
+    }
+    if (k < j) a0 = z_fms_conj<R>(z_ld<R>(row + k * ld), Lt[j + k * LDT], a0);
+    z_st<R>(row + j * ld, z_scale<R>(make_double2(a0.x + a1.x, a0.y + a1.y), rd[j]));
+  }
+}
+
+// S = L L^H in place (lower), panels of NB columns; V.rdiag[k] = 1 / L_kk.  Lt: NB x LDT tile.
+// Returns false (every thread) when S is not positive definite.
+template <bool R>
+__device__ bool cholesky_blocked(double2* __restrict__ A, int lda, int n, Vecs& V, double2* __restrict__ Lt) {
+  const int tid = threadIdx.x;
+  int* flag = reinterpret_cast<int*>(V.sc) + 2;
+  for (int c0 = 0; c0 < n; c0 += NB) {
+    const int w = min(NB, n - c0);
+    const int m = n - c0 - w;
+    double2* A11 = A + c0 + (int64_t)c0 * lda;
+    for (int e = tid; e < w * w; e += NT) {
+      const int i = e % w, j = e / w;
+      if (i >= j) Lt[i + j * LDT] = z_ld<R>(A11 + i + (int64_t)j * lda);
+    }
+    __syncthreads();
+    if (tid < 32) {             // unblocked Cholesky of the diagonal block, lane = row
+      const int lane = tid;
+      int bad = 0;
+      for (int k = 0; k < w; ++k) {
+        const double a = Lt[k + k * LDT].x;
+        const bool ok = (a > 0.0) && is_finite_bits(a);
+        bad |= ok ? 0 : 1;
+        const double dk = ok ? sqrt(a) : 1.0;
+        const double rd = 1.0 / dk;
+        __syncwarp();
+        if (lane == k) {
+          Lt[k + k * LDT] = make_double2(dk, 0.0);
+          V.rdiag[c0 + k] = rd;
+        }
+        double2 lik = make_double2(0.0, 0.0);
+        if (lane > k && lane < w) {
+          lik = z_scale<R>(Lt[lane + k * LDT], rd);
+          Lt[lane + k * LDT] = lik;
+        }
+        __syncwarp();
+        if (lane > k && lane < w)
+          for (int j = k + 1; j <= lane; ++j) Lt[lane + j * LDT] = z_fms_conj<R>(lik, Lt[j + k * LDT], Lt[lane + j * LDT]);
+        __syncwarp();
+      }
+      if (lane == 0) *flag = bad;
+    }
+    __syncthreads();
+    if (*flag) return false;
+    for (int e = tid; e < w * w; e += NT) {
+      const int i = e % w, j = e / w;
+      if (i >= j) z_st<R>(A11 + i + (int64_t)j * lda, Lt[i + j * LDT]);
+    }
+    if (m > 0) {                // here w == NB
+      double2* A21 = A11 + w;
+      for (int r = tid; r < m; r += NT) row_solve_lh<R>(A21 + r, lda, Lt, NB, V.rdiag + c0);
+      __syncthreads();
+      double2* A22 = A21 + (int64_t)w * lda;
+      const int tri = m * (m + 1) / 2;
+      for (int e = tid; e < tri; e += NT) {
+        int i, j;
+        tri_index(e, m, i, j);
+        double2* t = A22 + i + (int64_t)j * lda;
+        z_st<R>(t, panel_dot_conj<R>(A21 + i, lda, A21 + j, lda, z_ld<R>(t)));
+      }
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// A21 -= 1/2 L21 A11 for the m x NB panel, A11 Hermitian (both triangles) in the tile At.
+template <bool R>
+__device__ void panel_hemm_half(double2* __restrict__ A21, int lda, const double2* __restrict__ L21, int ldb, int m,
+                                const double2* __restrict__ At) {
+  for (int e = threadIdx.x; e < m * NB; e += NT) {
+    const int r = e % m, j = e / m;
+    double2 s0 = make_double2(0.0, 0.0), s1 = s0;
+#pragma unroll 8
+    for (int k = 0; k < NB; k += 2) {
+      s0 = z_fma<R>(z_ld<R>(L21 + r + (int64_t)k * ldb), At[k + j * LDT], s0);
+      s1 = z_fma<R>(z_ld<R>(L21 + r + (int64_t)(k + 1) * ldb), At[k + 1 + j * LDT], s1);
+    }
+    double2* t = A21 + r + (int64_t)j * lda;
+    z_st<R>(t, z_axpy<R>(-0.5, make_double2(s0.x + s1.x, s0.y + s1.y), z_ld<R>(t)));
+  }
+}
+
+// A (lower) <- L^-1 A L^-H with B = L from cholesky_blocked, LAPACK zhegst order per panel:
+// zhegs2 on the diagonal block, A21 L11^-H, -1/2 L21 A11, her2k A22 -= A21 L21^H + L21 A21^H,
+// -1/2 L21 A11, L22^-1 A21 (32-row chunks: a one-warp solve of the chunk, lanes over the NB
+// right-hand sides, then all threads update the rows below).  Lt, At: NB x LDT tiles.
+template <bool R>
+__device__ void hegst_blocked(double2* __restrict__ A, int lda, const double2* __restrict__ B, int ldb, int n,
+                              Vecs& V, double2* __restrict__ Lt, double2* __restrict__ At) {
+  const int tid = threadIdx.x;
+  for (int c0 = 0; c0 < n; c0 += NB) {
+    const int w = min(NB, n - c0);
+    const int m = n - c0 - w;
+    double2* A11 = A + c0 + (int64_t)c0 * lda;
+    const double2* L11 = B + c0 + (int64_t)c0 * ldb;
+    for (int e = tid; e < w * w; e += NT) {
+      const int i = e % w, j = e / w;
+      if (i >= j) {
+        Lt[i + j * LDT] = z_ld<R>(L11 + i + (int64_t)j * ldb);
+        At[i + j * LDT] = z_ld<R>(A11 + i + (int64_t)j * lda);
+      }
+    }
+    __syncthreads();
+    {
+      Vecs Vb = V;
+      Vb.rdiag = V.rdiag + c0;
+      hegs2_lower<R>(At, LDT, Lt, LDT, w, Vb, nullptr);   // ends with a barrier
+    }
+    for (int e = tid; e < w * w; e += NT) {
+      const int i = e % w, j = e / w;
+      if (i >= j) z_st<R>(A11 + i + (int64_t)j * lda, At[i + j * LDT]);
+    }
+    if (m == 0) break;
+    __syncthreads();
+    for (int e = tid; e < w * w; e += NT) {     // the reduced block as a full Hermitian tile
+      const int i = e % w, j = e / w;
+      if (i > j) {
+        const double2 v = At[i + j * LDT];
+        At[j + i * LDT] = make_double2(v.x, R ? 0.0 : -v.y);
+      }
+    }
+    double2* A21 = A11 + w;
+    const double2* L21 = L11 + w;
+    for (int r = tid; r < m; r += NT) row_solve_lh<R>(A21 + r, lda, Lt, NB, V.rdiag + c0);
+    __syncthreads();
+    panel_hemm_half<R>(A21, lda, L21, ldb, m, At);
+    __syncthreads();
+    double2* A22 = A21 + (int64_t)w * lda;
+    const int tri = m * (m + 1) / 2;
+    for (int e = tid; e < tri; e += NT) {
+      int i, j;
+      tri_index(e, m, i, j);
+      double2* t = A22 + i + (int64_t)j * lda;
+      double2 c = panel_dot_conj<R>(A21 + i, lda, L21 + j, ldb, z_ld<R>(t));
+      c = panel_dot_conj<R>(L21 + i, ldb, A21 + j, lda, c);
+      z_st<R>(t, c);
+    }
+    __syncthreads();
+    panel_hemm_half<R>(A21, lda, L21, ldb, m, At);
+    __syncthreads();
+    // A21 <- L22^-1 A21
+    const double2* L22 = L21 + (int64_t)w * ldb;
+    for (int r0 = 0; r0 < m; r0 += 32) {
+      const int cm = min(32, m - r0);
+      for (int e = tid; e < cm * cm; e += NT) {
+        const int i = e % cm, j = e / cm;
+        if (i >= j) Lt[i + j * LDT] = z_ld<R>(L22 + (r0 + i) + (int64_t)(r0 + j) * ldb);
+      }
+      for (int e = tid; e < cm * NB; e += NT) {
+        const int i = e % cm, j = e / cm;
+        At[i + j * LDT] = z_ld<R>(A21 + (r0 + i) + (int64_t)j * lda);
+      }
+      __syncthreads();
+      if (tid < NB) {
+        const int j = tid;
+        const double* rd = V.rdiag + c0 + w + r0;
+        for (int i = 0; i < cm; ++i) {
+          double2 a0 = At[i + j * LDT], a1 = make_double2(0.0, 0.0);
+          int q = 0;
+          for (; q + 1 < i; q += 2) {
+            a0 = z_sub_mul<R>(a0, Lt[i + q * LDT], At[q + j * LDT]);
+            a1 = z_sub_mul<R>(a1, Lt[i + (q + 1) * LDT], At[q + 1 + j * LDT]);
+          }
+          if (q < i) a0 = z_sub_mul<R>(a0, Lt[i + q * LDT], At[q + j * LDT]);
+          At[i + j * LDT] = z_scale<R>(make_double2(a0.x + a1.x, a0.y + a1.y), rd[i]);
+        }
+      }
+      __syncthreads();
+      for (int e = tid; e < cm * NB; e += NT) {
+        const int i = e % cm, j = e / cm;
+        z_st<R>(A21 + (r0 + i) + (int64_t)j * lda, At[i + j * LDT]);
+      }
+      const int rest = m - r0 - cm;
+      for (int e = tid; e < rest * NB; e += NT) {
+        const int r = e % rest, j = e / rest;
+        const double2* Lr = L22 + (r0 + cm + r) + (int64_t)r0 * ldb;
+        double2* t = A21 + (r0 + cm + r) + (int64_t)j * lda;
+        double2 a0 = z_ld<R>(t), a1 = make_double2(0.0, 0.0);
+        int q = 0;
+        for (; q + 1 < cm; q += 2) {
+          a0 = z_sub_mul<R>(a0, At[q + j * LDT], z_ld<R>(Lr + (int64_t)q * ldb));
+          a1 = z_sub_mul<R>(a1, At[q + 1 + j * LDT], z_ld<R>(Lr + (int64_t)(q + 1) * ldb));
+        }
+        if (q < cm) a0 = z_sub_mul<R>(a0, At[q + j * LDT], z_ld<R>(Lr + (int64_t)q * ldb));
+        z_st<R>(t, make_double2(a0.x + a1.x, a0.y + a1.y));
+      }
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+}
+
 // ------------------------------------------------------ tridiagonalisation
 // LAPACK zhetd2 (lower): reflector from column k, w = tau A22 v,
 // w -= (tau/2)(w^H v) v, A22 -= v w^H + w v^H.  d and e^2 go to shared memory.
@@ -541,7 +777,7 @@ __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const
                                                  const int32_t* __restrict__ order, double2* H, double2* S,
                                                  double* __restrict__ eig, int32_t* __restrict__ status,
                                                  int32_t* __restrict__ counter, int max_n, int use_smem_mats,
-                                                 double* __restrict__ tri_all) {
+                                                 double* __restrict__ tri_all, int64_t n_rows) {
   extern __shared__ double smem[];
   const int tid = threadIdx.x;
   Vecs V;
@@ -560,6 +796,7 @@ __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const
   }
   double2* Hs = reinterpret_cast<double2*>(smem + 16 + 4 * NW + 2 * NT + 3 * max_n + (max_n & 1) + 4 * max_n);
   double2* Ss = Hs + SMEM_LDA * SMEM_N;
+  double2* tileA = Hs + SMEM_REGION;      // second panel tile of the blocked factorisations
   __shared__ int s_idx;
   for (;;) {
     if (tid == 0) s_idx = atomicAdd(counter, 1);
@@ -569,6 +806,13 @@ __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const
     if (idx >= n_prob) break;
     const int p = order[idx];
     const int n = nvec[p];
+    // A problem larger than the launch's max_n would overrun the shared-memory vectors, and one whose
+    // eigenvalue rows end past n_rows would overrun the tridiagonal rows: refuse it, touch nothing.
+    if (n < 0 || n > max_n || eig_off[p] < 0 || eig_off[p] + n > n_rows) {
+      if (tid == 0) status[p] = SKN_ERR_CAPACITY;
+      __syncthreads();
+      continue;
+    }
     double2* Hg = H + hs_off[p];
     double2* Sg = S + hs_off[p];
     double2 *Ha, *Sa;
@@ -594,7 +838,9 @@ __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const
     aux_zero_rows(Ha, lda, n);
     aux_zero_rows(Sa, lda, n);
     __syncthreads();
-    const bool ok = cholesky_lower<R>(Sa, lda, n, V);
+    // problems staged in shared memory (n <= SMEM_N < NB) are one panel: the unblocked steps
+    const bool blocked = SKN_EIG_BLOCKED && !in_smem && n > NB;
+    const bool ok = blocked ? cholesky_blocked<R>(Sa, lda, n, V, Hs) : cholesky_lower<R>(Sa, lda, n, V);
     if (!ok) {
       for (int j = tid; j < n; j += NT) eig[eig_off[p] + j] = __longlong_as_double(0x7ff8000000000000LL);
       if (tid == 0) status[p] = SKN_ERR_NOT_SPD;
@@ -602,7 +848,10 @@ __global__ void __launch_bounds__(NT, SKN_EIG_MINB) k_eigh_gen(int n_prob, const
       continue;
     }
     double* tri = tri_all != nullptr ? tri_all + 4 * eig_off[p] : nullptr;
-    hegs2_lower<R>(Ha, lda, Sa, lda, n, V, in_smem ? nullptr : Hs);
+    if (blocked)
+      hegst_blocked<R>(Ha, lda, Sa, lda, n, V, Hs, tileA);
+    else
+      hegs2_lower<R>(Ha, lda, Sa, lda, n, V, in_smem ? nullptr : Hs);
     hetd2_lower<R>(Ha, lda, n, V, tri);
     if (n == 1 && tid == 0) V.d[0] = Ha[0].x;
     __syncthreads();
@@ -683,7 +932,9 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
     const int n = nvec[p];
     double2* Y = vec + hs_off[p];
     if (status[p] != SKN_OK) {
-      for (int q = tid; q < n * n; q += VNT) Y[q] = make_double2(__longlong_as_double(0x7ff8000000000000LL), 0.0);
+      // a problem the values kernel refused for its size keeps its buffers untouched
+      if (status[p] != SKN_ERR_CAPACITY)
+        for (int q = tid; q < n * n; q += VNT) Y[q] = make_double2(__longlong_as_double(0x7ff8000000000000LL), 0.0);
       __syncthreads();
       continue;
     }
@@ -861,7 +1112,7 @@ using namespace SKN_EIG_NS;
 // from several host threads never lower the limit under another's launch.
 static size_t eig_smem_bytes(int mn) {
   return sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn) +
-         SMEM_REGION * sizeof(double2);
+         (SMEM_REGION + (SKN_EIG_BLOCKED ? NB * LDT : 0)) * sizeof(double2);
 }
 static size_t vec_smem_bytes(int mn) {
   return sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;
@@ -896,7 +1147,7 @@ static int launch_values(int n_prob, const int32_t* n, const int64_t* hs_off, co
   if (grid > n_prob) grid = n_prob;
   if (cudaMemsetAsync(work_counter, 0, sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
   k_eigh_gen<R><<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig,
-                                            status, work_counter, mn, 1, nullptr);
+                                            status, work_counter, mn, 1, nullptr, INT64_MAX);
   return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
 }
 
@@ -961,8 +1212,7 @@ extern "C" int SKN_EXPORT(skn_eigh_gen_vectors)(int n_prob, const int32_t* n, co
   if (scratch_bytes < need) return SKN_ERR_CAPACITY;
   const int mn = max_n < 1 ? 1 : max_n;
   const int use_smem_mats = 1;
-  size_t smem = sizeof(double) * (16 + 4 * NW + 2 * NT + 3 * (size_t)mn + (mn & 1) + 4 * (size_t)mn);
-  smem += (size_t)use_smem_mats * SMEM_REGION * sizeof(double2);
+  const size_t smem = eig_smem_bytes(mn);
   if (set_smem_limit_once() != cudaSuccess) return SKN_ERR_CUDA;
   int per_sm = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -974,7 +1224,7 @@ extern "C" int SKN_EXPORT(skn_eigh_gen_vectors)(int n_prob, const int32_t* n, co
   if (grid > n_prob) grid = n_prob;
   if (cudaMemsetAsync(work_counter, 0, 2 * sizeof(int32_t), stream) != cudaSuccess) return SKN_ERR_CUDA;
   k_eigh_gen<false><<<grid, NT, smem, stream>>>(n_prob, n, hs_off, eig_off, order, (double2*)H, (double2*)S, eig, status,
-                                         work_counter, mn, use_smem_mats, tri);
+                                         work_counter, mn, use_smem_mats, tri, INT64_MAX);
   if (cudaPeekAtLastError() != cudaSuccess) return SKN_ERR_CUDA;
   const size_t vsmem = sizeof(double) * (2 * VNW + 2 * (size_t)mn + 2) + sizeof(double2) * (size_t)mn;
 
