@@ -3,12 +3,21 @@
 Requests (one periodic structure each) arrive at any time.  A request is
 admitted when its device-memory estimate fits the budget left by requests
 already admitted; admitted requests wait in a queue.  Each worker thread owns
-a CUDA stream: it takes every request that is admitted and not yet started
+a CUDA stream: it takes requests that are admitted and not yet started
 (up to ``max_batch_problems`` (structure, k) problems), plans them as one
 batch, runs the whole path on its stream, copies the results to the host and
 releases their memory.  With two or more workers, a batch formed from
 requests that arrived while another batch was on the GPU runs concurrently
 with it, so arrivals never wait for a whole batch to drain.
+
+Latency under load comes from small requests waiting behind large ones: a
+batch ends only when its largest eigensolve ends.  So requests are sorted
+into two lanes by orbital count (``large_orbitals``).  ``small_workers`` of
+the workers take small requests only; the others take large requests first
+and small ones when no large one waits.  Within a lane a worker takes the
+cheapest requests first (n^3 x k-points), and large problems run on the
+cluster eigensolver from ``large_threshold`` orbitals up, which shortens
+the longest eigensolve of a batch.
 
 The reference serves one structure per call (slakonet/optim.py:949-1075 via
 predict_slakonet.py); there is no queue, batch or stream there.
@@ -76,12 +85,23 @@ class Server:
                  species: Optional[Sequence[int]] = None, mem_budget_bytes: Optional[int] = None,
                  n_workers: int = 2, max_batch_problems: int = 8192, dos_range=(-20.0, 10.0),
                  dos_points: int = 1000, dos_sigma: float = 0.1, dos_window: float = 9.0,
-                 executor: Optional[Callable] = None):
+                 executor: Optional[Callable] = None, large_orbitals: Optional[int] = 256,
+                 small_workers: Optional[int] = None, large_threshold: Optional[int] = 512):
         self.model = model
         self.sd = shell_dict
         self.device = torch.device(device)
         self.dos = dict(dos_range=dos_range, dos_points=dos_points, dos_sigma=dos_sigma, dos_window=dos_window)
         self.max_batch_problems = max_batch_problems
+        # size lanes: requests above large_orbitals are "large"; the first small_workers workers take
+        # small requests only (None: all but one worker when there are at least two; no lanes when
+        # large_orbitals is None)
+        self.large_orbitals = large_orbitals
+        if large_orbitals is None:
+            small_workers = 0
+        elif small_workers is None:
+            small_workers = n_workers - 1 if n_workers >= 2 else 0
+        self.small_workers = max(0, min(int(small_workers), n_workers - 1))
+        self.large_threshold = large_threshold
         if mem_budget_bytes is None:
             free, _ = torch.cuda.mem_get_info(self.device)
             mem_budget_bytes = int(0.6 * free)
@@ -167,22 +187,39 @@ class Server:
                     if self.stop:
                         return
 
-    def _take_batch(self) -> List[Request]:
+    def is_large(self, r: Request) -> bool:
+        return self.large_orbitals is not None and r.n_orb > self.large_orbitals
+
+    def _take_batch(self, worker: int = -1) -> List[Request]:
+        """The requests of a worker's next batch: its lane's ready requests, cheapest first (n^3 x nk),
+        up to max_batch_problems problems.  A small-lane worker takes small requests only; any other
+        worker takes large requests when one waits, else small ones."""
+        small_only = 0 <= worker < self.small_workers
         with self.cv:
-            while not self.ready and not self.stop:
+            while True:
+                if small_only:
+                    cand = [r for r in self.ready if not self.is_large(r)]
+                else:
+                    cand = [r for r in self.ready if self.is_large(r)] or list(self.ready)
+                if cand or self.stop:
+                    break
                 self.cv.wait(0.05)
-            if not self.ready:
+            if not cand:
                 return []
+            cand.sort(key=lambda r: (float(r.n_orb) ** 3 * r.nk, r.rid))
             batch, probs = [], 0
-            while self.ready and (not batch or probs + self.ready[0].nk <= self.max_batch_problems):
-                r = self.ready.pop(0)
+            for r in cand:
+                if batch and probs + r.nk > self.max_batch_problems:
+                    break
                 probs += r.nk
                 batch.append(r)
+            taken = {id(r) for r in batch}
+            self.ready = [r for r in self.ready if id(r) not in taken]
             return batch
 
     def _execute(self, structures, stream):
         with torch.cuda.stream(stream):
-            eng = E.Engine(self.tables, stream=stream)
+            eng = E.Engine(self.tables, stream=stream, large_threshold=self.large_threshold)
             plan = E.plan_batch(structures, self.tables)
             db = E.DeviceBatch(plan, self.device)
             res = eng.execute(db, **self.dos)
@@ -204,11 +241,13 @@ class Server:
     def _worker(self, idx: int):
         stream = torch.cuda.Stream(self.device) if self.executor == self._execute else None
         while True:
-            batch = self._take_batch()
+            batch = self._take_batch(idx)
             if not batch:
                 with self.cv:
                     if self.stop and not self.ready:
                         return
+                    if self.stop and idx < self.small_workers:
+                        return           # what is left is large: a worker of the other lane takes it
                 continue
             # claim each future: one a client cancelled while it waited is dropped here (its memory
             # released), and none can be cancelled once its batch runs

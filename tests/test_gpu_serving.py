@@ -29,6 +29,10 @@ def test_results_identical_alone_and_in_the_mix():
         sts.insert(pos, st)
     zs = sorted({int(z) for st in sts for z in st["numbers"]})
     sd = syn.default_shell_dict()
+    # the server sends problems above 512 orbitals to the cluster eigensolver, compute_properties_batch those
+    # above 1024: no structure here falls between, so both run every problem on the same kernel
+    norb = [sum(sum(2 * l + 1 for l in sd[int(z)]) for z in st["numbers"]) for st in sts]
+    assert not any(512 < n <= 1024 for n in norb)
     tables = syn.make_tables(zs, sd, seed=4)
     model = M.MultiElementSkfParameterOptimizer.from_tables(tables)
     server = SV.Server(model, sd, DEV, species=zs, n_workers=3, mem_budget_bytes=1 << 30)

@@ -161,7 +161,7 @@ def test_executor_failure_reaches_every_request_of_its_batch_and_serving_continu
     after = server.submit(_atoms(4))
     assert after.result(timeout=10)["n"] == 4             # the worker survived the failed batch
     server.close()
-    assert seen == [[1], [2, 7, 3], [4]]
+    assert seen == [[1], [2, 3, 7], [4]]                 # the batch runs cheapest first
     assert server.adm.used == 0                          # every request's memory was released
 
 
@@ -220,3 +220,38 @@ def test_serving_request_file_round_trip_and_bench_loader(tmp_path):
     assert source == path and _same(sts, got)
     with pytest.raises(SystemExit):
         bench.serving_set(4, path)
+
+
+def test_size_lanes_keep_large_requests_off_the_small_lane_and_take_the_cheapest_first():
+    """Three workers: two take small requests only, the third takes large ones first.  Every batch is
+    ordered cheapest first (orbitals^3 x k-points), and every request completes."""
+    sd = syn.default_shell_dict()
+    norb = lambda st: sum(sum(2 * l + 1 for l in sd[int(z)]) for z in st["numbers"])
+    taken, lock = [], threading.Lock()
+
+    def fake_exec(structures, stream):
+        w = server.workers.index(threading.current_thread())
+        with lock:
+            taken.append((w, [float(norb(st)) ** 3 * len(st["kpoints"]) for st in structures],
+                          [norb(st) for st in structures]))
+        time.sleep(0.005)
+        return [{"eigenvalues": np.zeros(1), "band_gap_eV": 0.0} for _ in structures]
+
+    rng = np.random.default_rng(5)
+    sts = _structs(40, seed=5)
+    for pos in (3, 11, 19, 30):                     # 40 atoms of Z = 21..30: 360 orbitals, above the 256 line
+        st = syn.random_structure(rng, 40, zmax=30)
+        st["numbers"] = 21 + (np.asarray(st["numbers"]) % 10)
+        st["kpoints"] = np.zeros((2, 3))
+        sts.insert(pos, st)
+    server = SV.Server(FakeModel(), sd, device="cpu", mem_budget_bytes=1 << 40, n_workers=3, executor=fake_exec)
+    assert server.small_workers == 2
+    lat, wall, res = SV.poisson_stream(server, sts, rate=5000.0, seed=3)
+    server.close()
+    assert len(lat) == len(sts)
+    assert sum(len(n) for _, _, n in taken) == len(sts)
+    for w, cost, n in taken:
+        if w < 2:
+            assert max(n) <= 256
+        assert cost == sorted(cost)
+    assert any(max(n) > 256 for w, _, n in taken if w == 2)
