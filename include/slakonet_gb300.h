@@ -386,6 +386,36 @@ int skn_fp64_probe(double* out, int blocks, int iters, cudaStream_t stream);
  */
 int skn_fp64_probe_dmma(double* out, int blocks, int iters, cudaStream_t stream);
 
+/*
+ * bf16 tensor-core GEMM (tcgen05, TMEM accumulators), no reference
+ * counterpart: D[M x N] = A B^T in FP32, A [M x K] and B [N x K] bf16 with K
+ * contiguous (raw bf16 bit patterns), D row-major.  M and N multiples of 128,
+ * K a multiple of 64, pointers 16-byte aligned (else SKN_ERR_ARG).  *err is
+ * set to 1 when a stage's completion wait exceeded its iteration limit.  The
+ * building block of the FP64 emulation below; with integer operands of at
+ * most 8 significant bits and K <= 256 every product and partial sum is an
+ * integer below 2^24, which an exact FP32 accumulator holds without rounding.
+ */
+int skn_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, int32_t* err,
+                     cudaStream_t stream);
+
+/*
+ * FP64 GEMM C[M x N] = A B^T (A [M x K], B [N x K], FP64 row-major, K
+ * contiguous) computed on the bf16 tensor cores by error-free splitting into
+ * `slices` (1..8) integer bf16 slices per operand row (Ozaki, Ogita and
+ * Oishi 2012): the slice products with s + t < slices, each exact in FP32 for
+ * K chunks of 256, are scaled by powers of two and summed in FP64.  With 7
+ * slices the result agrees with an FP64 GEMM to FP64 rounding.  No reference
+ * counterpart: GB300's FP64 tensor instruction runs no faster than FP64 FMA,
+ * so this is the tensor-core route for the eigensolver's GEMM-shaped FP64
+ * updates.  M, N multiples of 128, K a multiple of 256.
+ *   scratch  device buffer of skn_gemm_f64_emulated_scratch_bytes bytes
+ */
+int skn_gemm_f64_emulated(const double* A, const double* B, double* C, int M, int N, int K, int slices,
+                          void* scratch, int64_t scratch_bytes, int32_t* err, cudaStream_t stream);
+/* Host-side query: scratch bytes skn_gemm_f64_emulated needs (written to *bytes). */
+int skn_gemm_f64_emulated_scratch_bytes(int M, int N, int K, int slices, int64_t* bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,6 +46,9 @@ SIGNATURES = {
     "skn_dos": [I32, P, P, P, P, P, P, P, F64, F64, I32, F64, F64, P, P, P, P],
     "skn_fp64_probe": [P, I32, I32, P],
     "skn_fp64_probe_dmma": [P, I32, I32, P],
+    "skn_tc_gemm_bf16": [P, P, P, I32, I32, I32, P, P],
+    "skn_gemm_f64_emulated": [P, P, P, I32, I32, I32, I32, P, I64, P, P],
+    "skn_gemm_f64_emulated_scratch_bytes": [I32, I32, I32, I32, P],
     "skn_eigh_gen_vectors": [I32, P, P, P, P, P, P, P, P, P, P, P, I64, P, I32, P],
     "skn_eigh_vectors_scratch_bytes": [I32, I32, P],
     "skn_eigh_gen_vectors_noalloc": [I32, P, P, P, P, P, P, P, P, P, I64, I32, P],
