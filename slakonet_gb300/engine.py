@@ -461,6 +461,12 @@ def cluster_for(n: int) -> int:
     return 4 if n <= 2048 else (8 if n <= 4096 else 12)
 
 
+def _default_tuning():
+    """Launch shapes per size bucket when the engine has no autotuned ones (autotune.Tuning.default)."""
+    from .autotune import Tuning
+    return Tuning.default()
+
+
 def route_large(prob_n: np.ndarray, threshold: Optional[int] = 1024, cluster: Optional[int] = None) -> np.ndarray:
     """Cluster size per problem, 0 for the one-CTA-per-problem eigensolver.
 
@@ -529,9 +535,11 @@ class Engine:
         return self.tail(db, bonds, dos_range, dos_points, dos_sigma, dos_window, keep_hs, hs_only, vectors,
                          keep_state)
 
-    def bonds(self, db: DeviceBatch) -> dict:
+    def bonds(self, db: DeviceBatch, out: Optional[dict] = None) -> dict:
         """Neighbour list: counts, host scan (one device->host read), fill.  The result is the
-        structure-only part of the path and stays valid while the geometry does."""
+        structure-only part of the path and stays valid while the geometry does.  With ``out``
+        (an earlier result for the same geometry, e.g. the buffers a captured graph reads) the
+        list is rebuilt into those buffers; a count that differs from theirs raises."""
         plan = db.plan
         dev = self.device
         S = plan.n_struct
@@ -546,16 +554,24 @@ class Engine:
         np.cumsum(cnt * plan.pair_ni_nj, out=pair_blk[1:])
         nbond = int(pair_ptr[-1])
         nblk = int(pair_blk[-1])
-        d_pair_ptr = _i64(pair_ptr, dev)
-        d_pair_blk = _i64(pair_blk[:-1] if plan.n_pairs else np.zeros(1), dev)
-        nb1 = max(nbond, 1)
-        b = dict(nbond=nbond, nblk=nblk, pair_ptr=d_pair_ptr,
-                 bond_i=torch.empty(nb1, dtype=torch.int32, device=dev),
-                 bond_j=torch.empty(nb1, dtype=torch.int32, device=dev),
-                 bond_img=torch.empty(nb1, dtype=torch.int32, device=dev),
-                 bond_d=torch.empty(nb1, dtype=torch.float64, device=dev),
-                 bond_u=torch.empty(3 * nb1, dtype=torch.float64, device=dev),
-                 bond_blk=torch.empty(nb1, dtype=torch.int64, device=dev))
+        if out is not None:
+            if out["nbond"] != nbond or out["nblk"] != nblk:
+                raise ValueError("the neighbour list changed size: the geometry is not the captured one")
+            b = out
+            b["pair_ptr"].copy_(torch.from_numpy(pair_ptr), non_blocking=False)
+            d_pair_blk = _i64(pair_blk[:-1] if plan.n_pairs else np.zeros(1), dev)
+            d_pair_ptr = b["pair_ptr"]
+        else:
+            d_pair_ptr = _i64(pair_ptr, dev)
+            d_pair_blk = _i64(pair_blk[:-1] if plan.n_pairs else np.zeros(1), dev)
+            nb1 = max(nbond, 1)
+            b = dict(nbond=nbond, nblk=nblk, pair_ptr=d_pair_ptr,
+                     bond_i=torch.empty(nb1, dtype=torch.int32, device=dev),
+                     bond_j=torch.empty(nb1, dtype=torch.int32, device=dev),
+                     bond_img=torch.empty(nb1, dtype=torch.int32, device=dev),
+                     bond_d=torch.empty(nb1, dtype=torch.float64, device=dev),
+                     bond_u=torch.empty(3 * nb1, dtype=torch.float64, device=dev),
+                     bond_blk=torch.empty(nb1, dtype=torch.int64, device=dev))
         self._call("skn_bond_fill", S, plan.n_pairs, ptr(db.atom_ptr), ptr(db.pos), ptr(db.cells), ptr(db.rng),
                    self.cutoff, ptr(db.pair_base), ptr(d_pair_ptr), ptr(d_pair_blk), ptr(db.norb), ptr(b["bond_i"]),
                    ptr(b["bond_j"]), ptr(b["bond_img"]), ptr(b["bond_d"]), ptr(b["bond_u"]), ptr(b["bond_blk"]),
@@ -717,10 +733,8 @@ class Engine:
             out.append((int(c), _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))
         small_order = plan.order[~large]
         if len(small_order):
-            if self.tuning is None:
-                shapes = [""] * len(small_order)
-            else:
-                shapes = [self.tuning.shape_for(int(n)) for n in plan.prob_n[small_order]]
+            tuning = self.tuning if self.tuning is not None else _default_tuning()
+            shapes = [tuning.shape_for(int(n)) for n in plan.prob_n[small_order]]
             if self.real_path and plan.prob_real is not None:
                 shapes = [("_real" + sh) if r else sh for sh, r in zip(shapes, plan.prob_real[small_order])]
             shapes = np.array(shapes, dtype=object)
