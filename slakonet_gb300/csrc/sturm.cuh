@@ -146,8 +146,10 @@ __device__ double eigenvalue(const double* d, const double* e2, const float* d32
       if (c > j) b = x; else a = x;
       if (b - a <= B.atol) break;
       const double xn = x - step;
+      // converged: the last step may land on the bracket's edge (the root lies within rounding of
+      // the point just counted), so it is tested before the bracket, not after
+      if (fabs(step) <= B.atol && xn >= a && xn <= b) return xn;
       if (xn > a && xn < b && fabs(step) <= 0.5 * dx_old) {
-        if (fabs(step) <= B.atol) return xn;
         dx_old = fabs(step);
         x = xn;
       } else {
