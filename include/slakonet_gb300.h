@@ -238,6 +238,32 @@ int skn_eigh_gen_large(int n_prob, const int32_t* n, const int64_t* hs_off, cons
 int skn_eigh_large_scratch_bytes(int n_prob, int max_n, int cluster, int64_t* bytes);
 
 /*
+ * Eigenvalues of large problems with the whole GPU: blocked (32-column panels)
+ * Cholesky, zhegst-order reduction and zlatrd-order tridiagonalisation, each
+ * step one kernel launch across all problems of the group, with tiled rank-2k
+ * updates and a tiled Hermitian matrix-vector product, then Sturm-count
+ * eigenvalues.  Replaces the same eighb call as skn_eigh_gen_batched
+ * (slakonet/utils.py:741-783) for problems too large for one SM, without the
+ * cluster path's bound of 16 SMs per problem.  The host issues about 6n + 9n/32
+ * launches on `stream`, so it suits problems of more than ~1000 orbitals.
+ *   n_prob    problems in the group (<= 32767); all must have n orbitals
+ *   n         orbitals of every problem (host value, 1..32768)
+ *   prob      [n_prob] (device) problem index of each group slot, into the arrays below
+ *   nvec, hs_off, eig_off, H, S, eig, status   as skn_eigh_gen_batched; a problem
+ *             whose nvec differs from n gets SKN_ERR_CAPACITY and is not touched
+ *   scratch   device scratch of skn_eigh_wide_scratch_bytes(n_prob, n) bytes
+ *   real      1 when every problem's H and S are exactly real (their imaginary
+ *             parts are then neither read nor written), else 0
+ * Results depend only on each problem: every cross-CTA sum is reduced in a
+ * fixed order.  H and S are overwritten; the upper triangles are not read.
+ */
+int skn_eigh_gen_wide(int n_prob, int n, const int32_t* prob, const int32_t* nvec, const int64_t* hs_off,
+                      const int64_t* eig_off, double* H, double* S, double* eig, int32_t* status, double* scratch,
+                      int64_t scratch_bytes, int real, cudaStream_t stream);
+/* Host-side query: bytes of `scratch` skn_eigh_gen_wide needs (written to *bytes). */
+int skn_eigh_wide_scratch_bytes(int n_prob, int n, int64_t* bytes);
+
+/*
  * The same eigensolver compiled in two more launch shapes: 64 threads per CTA
  * with up to 8 CTAs per SM (suffix _t64), and 256 threads with up to 3 CTAs per
  * SM (suffix _t256).  The unsuffixed entry points use 128 threads and up to 5

@@ -443,6 +443,20 @@ KERNELS_PER_CALL = {"skn_bond_counts": 1, "skn_bond_fill": 1, "skn_image_phases"
                     "skn_bloch": 1, "skn_eigh_gen_batched": 1, "skn_eigh_gen_vectors": 2, "skn_fermi_gap": 1,
                     "skn_dos": 2, "skn_eigh_gen_large": 1, "skn_eigh_gen_vectors_noalloc": 2}
 
+def wide_launches(n: int, nb: int = 32, ts: int = 64) -> int:
+    """Kernel launches of one skn_eigh_gen_wide call for problems of n orbitals (its host sequence)."""
+    T = -(-n // nb)
+    k = 3 + T + 2 * (T - 1)                   # set-up; Cholesky: diagonal blocks, row solves + updates
+    k += T + 4 * (T - 1)                      # reduction: diagonal blocks; solve, two hemm, rank-2k
+    k += (T - 1) + sum(1 for t in range(1, T) if (t + 1) * nb < n)   # deferred solves
+    c0 = 0
+    while c0 < n - 1:                         # tridiagonalisation: 6 per column, 1 per panel update
+        w = min(nb, n - 1 - c0)
+        k += 6 * w + (1 if n - c0 - w > 0 else 0)
+        c0 += nb
+    return k + 2                              # bounds and eigenvalues
+
+
 _SIDE = threading.local()   # per-thread side streams of Engine._side_streams
 
 SINGLE_CTA_MAX_N = 2048   # bound of the one-CTA-per-problem eigensolver (csrc/eigh.cu)
@@ -459,6 +473,16 @@ def cluster_for(n: int) -> int:
     2048 orbitals; 8 up to 4096; above that 12, so that a structure's 8 k-points (a 2x2x2
     grid) all run at once."""
     return 4 if n <= 2048 else (8 if n <= 4096 else 12)
+
+
+def route_wide(prob_n: np.ndarray, threshold: Optional[int]) -> np.ndarray:
+    """True for problems the device-wide eigensolver takes (csrc/eigh_wide.cu): more than
+    ``threshold`` orbitals (None: none).  Like route_large, the choice depends on each problem
+    alone, and the wide path's results depend only on the problem, so a structure's results are
+    bitwise the same whatever it is batched with."""
+    if threshold is None:
+        return np.zeros(len(prob_n), dtype=bool)
+    return prob_n.astype(np.int64) > int(threshold)
 
 
 def _default_tuning():
@@ -489,7 +513,7 @@ class Engine:
 
     def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None,
                  tuning=None, large_threshold: Optional[int] = 1024, large_cluster: Optional[int] = None,
-                 real_path: bool = True):
+                 real_path: bool = True, wide_threshold: Optional[int] = None):
         _dev(tables.device)
         self.tables = tables
         self.tuning = tuning          # autotune.Tuning: eigensolver launch shape per problem-size bucket
@@ -497,6 +521,8 @@ class Engine:
         # see route_large (large_cluster None: cluster_for(n))
         self.large_threshold = large_threshold
         self.large_cluster = large_cluster
+        # problems above wide_threshold orbitals run on the device-wide eigensolver instead (route_wide)
+        self.wide_threshold = wide_threshold
         # values-only solves of problems with exactly real H(k), S(k) use the real-arithmetic
         # kernel (skn_eigh_gen_batched_real): same numbers, a quarter of the FP64 work
         self.real_path = bool(real_path)
@@ -516,7 +542,7 @@ class Engine:
         if ev is not None:
             b.record()
             ev.append((name, a, b))
-        self.launches += KERNELS_PER_CALL.get(name, 1)
+        self.launches += wide_launches(args[1]) if name == "skn_eigh_gen_wide" else KERNELS_PER_CALL.get(name, 1)
 
     def run(self, plan: Plan, dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
             dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False,
@@ -669,14 +695,22 @@ class Engine:
             return
         scratch = {}
         for gi, (shape, _, count, max_n) in enumerate(groups):
+            need = ctypes.c_int64(0)
             if isinstance(shape, int):       # a cluster group
-                need = ctypes.c_int64(0)
                 call("skn_eigh_large_scratch_bytes", count, max_n, shape, ctypes.addressof(need))
-                scratch[gi] = torch.empty(max(need.value // 8, 1), dtype=torch.float64, device=self.device)
+            elif isinstance(shape, tuple):   # a device-wide group: ("wide", n, real)
+                call("skn_eigh_wide_scratch_bytes", count, max_n, ctypes.addressof(need))
+            else:
+                continue
+            scratch[gi] = torch.empty(max(need.value // 8, 1), dtype=torch.float64, device=self.device)
         counters = torch.zeros(2 * len(groups), dtype=torch.int32, device=self.device)
 
         def launch(gi, sfx, order_g, count, max_n, st):
-            if isinstance(sfx, int):
+            if isinstance(sfx, tuple):
+                self._call("skn_eigh_gen_wide", count, max_n, ptr(order_g), ptr(db.n), ptr(db.hs_off), ptr(db.eoff),
+                           ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(scratch[gi]),
+                           int(scratch[gi].numel() * 8), int(sfx[2]), st)
+            elif isinstance(sfx, int):
                 self._call("skn_eigh_gen_large", count, ptr(db.n), ptr(db.hs_off), ptr(db.eoff), ptr(order_g),
                            ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(counters[2 * gi:]), ptr(scratch[gi]),
                            int(scratch[gi].numel() * 8), max_n, sfx, st)
@@ -716,19 +750,28 @@ class Engine:
         return cur
 
     def _groups(self, db):
-        """[(launch shape suffix, or the cluster size for the cluster path, device order, count, max_n)],
-        cached on the batch.
+        """[(launch shape suffix, the cluster size for the cluster path, or ("wide", n, real) for the
+        device-wide path, device order, count, max_n)], cached on the batch.
 
         Empty when every problem takes the default single-CTA launch."""
         plan = db.plan
-        key = (id(self.tuning), self.large_threshold, self.large_cluster, self.real_path)
+        key = (id(self.tuning), self.large_threshold, self.large_cluster, self.real_path, self.wide_threshold)
         cache = getattr(db, "_groups", None)
         if cache is not None and cache[0] == key:
             return cache[1]
+        wide = route_wide(plan.prob_n, self.wide_threshold)[plan.order]
         csize = route_large(plan.prob_n, self.large_threshold, self.large_cluster)[plan.order]
-        large = csize > 0
+        csize[wide] = 0
+        large = (csize > 0) | wide
         out = []
-        for c in sorted(set(csize[large].tolist()), reverse=True):    # one launch per cluster size
+        if wide.any():                       # one group per (n, real), largest first
+            wn = plan.prob_n[plan.order[wide]]
+            wr = (plan.prob_real[plan.order[wide]] if (self.real_path and plan.prob_real is not None)
+                  else np.zeros(len(wn), dtype=bool))
+            for n_, r_ in sorted({(int(a), bool(b)) for a, b in zip(wn, wr)}, reverse=True):
+                sel = plan.order[wide][(wn == n_) & (wr == r_)]
+                out.append((("wide", n_, int(r_)), _i32(sel, self.device), len(sel), n_))
+        for c in sorted(set(csize[csize > 0].tolist()), reverse=True):    # one launch per cluster size
             sel = plan.order[csize == c]
             out.append((int(c), _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))
         small_order = plan.order[~large]

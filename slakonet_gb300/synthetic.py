@@ -217,18 +217,20 @@ def random_structure(rng: np.random.Generator, n_atoms: int, zmax: int = 65,
         cell = _cell_from_params(*edges, *ang)
         if cell is None:
             continue
-        frac = []
+        frac = np.empty((n_atoms, 3))
+        placed_n = 0
         ok = True
         shifts = np.array([[i, j, k] for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)], float)
         for _ in range(n_atoms):
             placed = False
             for _t in range(max_tries):
                 f = rng.uniform(0.0, 1.0, 3)
-                if frac:
-                    d = (np.array(frac)[:, None, :] - f[None, None, :] + shifts[None]) @ cell
+                if placed_n:
+                    d = (frac[:placed_n, None, :] - f[None, None, :] + shifts[None]) @ cell
                     if np.sqrt((d * d).sum(-1)).min() < dmin:
                         continue
-                frac.append(f)
+                frac[placed_n] = f
+                placed_n += 1
                 placed = True
                 break
             if not placed:
@@ -237,7 +239,7 @@ def random_structure(rng: np.random.Generator, n_atoms: int, zmax: int = 65,
         if ok:
             break
     numbers = rng.integers(1, zmax + 1, n_atoms)
-    pos = np.array(frac) @ cell
+    pos = frac @ cell
     return {"numbers": numbers, "positions": pos, "cell": cell}
 
 
