@@ -43,11 +43,18 @@ DOS_POINTS = 1000
 DOS_SIGMA = 0.1
 DOS_WINDOW = 9.0
 SAMPLE_STRIDE = 16         # CPU baseline: every 16th structure (stratified over sizes)
-# DRAM bytes (read + write) of one eigensolver launch on the default workload (256 structures, seed 0),
-# from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_eigh_gen`
-# on `bench.py --steps 1 --warmup 1 --no-cpu-baseline --no-extras` (one pass per launch): 0.950 TB read +
-# 0.509 TB written per launch
-EIG_TRAFFIC_BYTES = 1.459e12
+# DRAM bytes (read + write) of the eigensolver launches of one execution, measured by ncu on two
+# stratified samples of the default workload (profiles/k_eigh_gen_uneven_samples_dram.md):
+# `ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
+#  -k regex:k_eigh_gen -s 4 -c 4 python bench.py --path-only --sample-stride K --steps 1 --warmup 1`.
+# The ratio to the H(k)+S(k) bytes grows with the number of large problems in flight (L2 holds fewer of
+# their trailing matrices), so it is not scaled to the full batch, whose capture the size rule excludes.
+EIG_TRAFFIC_SAMPLES = {
+    "every 16th structure by size (16 structures, 1877 problems)":
+        {"hs_bytes": 659664384, "dram_bytes": 1564348928, "ncu_ms": 520.9},
+    "every 4th structure by size (64 structures, 8424 problems)":
+        {"hs_bytes": 2215006848, "dram_bytes": 37161698048, "ncu_ms": 564.8},
+}
 WORKLOAD = ("uneven batch: 256 random periodic structures, 2-64 atoms log-uniform, Z=1-65 default shells, "
             "Gamma-centred k-grids ~1000 k-atoms, FP64 generalized eigensolve per k, Fermi/gap, "
             "1000-pt DOS on [-20,10] eV")
@@ -344,23 +351,13 @@ def measured_hbm_gbs(peaks_path=PEAKS_PATH):
         return None
 
 
-def hbm_context(traffic_bytes, seconds, peaks_path=PEAKS_PATH):
-    """DRAM rate of one launch (ncu traffic / CUDA-event time) against the measured HBM copy peak,
-    or None when either number is missing."""
-    peak = measured_hbm_gbs(peaks_path)
-    if not traffic_bytes or not seconds or not peak:
-        return None
-    gbs = traffic_bytes / seconds / 1e9
-    return {"achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
-
-
-def bloch_roofline(seconds_per_step, hs_total, peaks_path=PEAKS_PATH):
-    """k_bloch is bound by its HBM writes: H(k) and S(k), 16 bytes per complex element each, so
-    2 * 16 * (sum of n^2 over the step's problems) algorithmic bytes per step."""
+def bloch_roofline(seconds_per_step, elements, peaks_path=PEAKS_PATH):
+    """The Bloch stage against HBM: it writes H(k) and S(k), 16 bytes per complex element each, so
+    2 * 16 * ``elements`` algorithmic bytes per step (``elements``: the complex entries formed per step,
+    n(n+1)/2 per problem for the lower triangles the eigensolvers read)."""
     if not seconds_per_step:
         return None
-    nbytes = 2 * 16 * int(hs_total)
+    nbytes = 2 * 16 * int(elements)
     gbs = nbytes / seconds_per_step / 1e9
     peak = measured_hbm_gbs(peaks_path)
     return {"bound": "hbm", "bytes_per_step": nbytes, "ms_per_step": 1e3 * seconds_per_step, "achieved_gbs": gbs,
@@ -492,6 +489,7 @@ def run_gpu(args, rank, world):
     eig_t = statistics.mean(per_call["eigensolve"])
     achieved = flops_eig / eig_t / 1e12
     shares = {k: round(sum(v) / elapsed_u, 4) for k, v in per_call.items()}
+    lower_elems = int(np.sum(plan.prob_n.astype(np.int64) * (plan.prob_n.astype(np.int64) + 1) // 2))
     if rank != 0:
         return None
     out = {
@@ -512,21 +510,23 @@ def run_gpu(args, rank, world):
                    "autotune_batch_trials_ms": tuning.timings.get("batch_trials_ms")},
         "roofline": {"bound": "tensor", "kernel": "k_eigh_gen (skn_eigh_gen_batched, autotuned launch shapes)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": (EIG_TRAFFIC_BYTES if (args.structures, args.seed) == (N_STRUCT, SEED)
-                                 else None),
-                     "traffic_note": "DRAM bytes per eigensolver launch (ncu); H(k)+S(k) are "
-                                     f"{2 * 16 * plan.hs_total / 1e9:.1f} GB, re-streamed from HBM every column "
-                                     "pass because the 760 problems in flight hold more than L2",
+                     "traffic": None,
+                     "traffic_note": "not captured on the full batch (the capture-size rule); measured on two "
+                                     "stratified samples, see traffic_samples: DRAM bytes per execution of the "
+                                     "eigensolver launches against their H(k)+S(k) bytes. The kernel is FP64-bound: "
+                                     "its DRAM rate in the larger sample is about 1% of HBM",
+                     "traffic_samples": {k: dict(v, ratio=round(v["dram_bytes"] / v["hs_bytes"], 2),
+                                                 dram_gbs=round(v["dram_bytes"] / v["ncu_ms"] / 1e6, 1))
+                                         for k, v in EIG_TRAFFIC_SAMPLES.items()},
                      "peak_source": "measured in this run: FP64 FMA probe kernel (skn_fp64_probe); the FP64 "
                                     "tensor instruction (skn_fp64_probe_dmma) is measured beside it",
                      "fp64_fma_tflops": peak, "fp64_dmma_tflops": peak_dmma,
                      "algorithmic": "32/3 n^3 real flops per complex k-point (zpotrf 4/3 + zhegst 4 + zhetrd 16/3), "
                                     "8/3 n^3 per real one (2k integer: dpotrf + dsygst + dsytrd)",
                      "real_k_points": int(plan.prob_real.sum()),
-                     "hbm": hbm_context(EIG_TRAFFIC_BYTES if (args.structures, args.seed) == (N_STRUCT, SEED)
-                                        else None, eig_t),
-                     "stages": {"bloch": bloch_roofline(sum(per_call.get("skn_bloch", [])) / args.steps,
-                                                        plan.hs_total)},
+                     "stages": {"bloch": dict(bloch_roofline(sum(per_call.get("skn_bloch_pairs", [])) / args.steps,
+                                                             lower_elems) or {},
+                                              kernel="k_bloch_pairs (skn_bloch_pairs, lower triangles)")},
                      "eig_kernel_ms": eig_t * 1e3, "time_share": shares},
         "e2e": {"value": job_rate(world, solves, args.steps, e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e / args.steps},
@@ -638,10 +638,76 @@ def run_serving(dev, n_requests=200, rate=4.0, seq_sample=40, capacity=True, pat
                         "each response: eigenvalues, DOS, gap, Fermi level"}
 
 
+def run_path_only(args):
+    """The path alone for profiling: the workload (every ``--sample-stride``-th structure by size when
+    given), default launch shapes (no autotuning), ``--warmup`` then ``--steps`` executions of the whole
+    path on one stream, no graph capture and no extras.  Prints kernel launches per execution, so an ncu
+    run can skip the warm-up launches (-s) and capture one execution (-c)."""
+    import torch
+    from slakonet_gb300 import engine as E, model as M
+    import __graft_entry__ as ge
+    ge.build()
+    dev = torch.device("cuda", 0)
+    sts, tables, sd = workload(args.structures, args.seed)
+    if args.sample_stride:
+        sts = [sts[i] for i in cpu_sample_indices(sts, args.sample_stride)]
+    model = M.MultiElementSkfParameterOptimizer.from_tables(tables)
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    ts = model.table_set(sd, dev, zs)
+    plan = E.plan_batch(sts, ts)
+    eng = E.Engine(ts)
+    db = E.DeviceBatch(plan, dev)
+    kw = dict(dos_range=DOS_RANGE, dos_points=DOS_POINTS, dos_sigma=DOS_SIGMA, dos_window=DOS_WINDOW)
+    for _ in range(args.warmup):
+        eng.execute(db, **kw)
+    torch.cuda.synchronize(dev)
+    l0 = eng.launches
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        eng.execute(db, **kw)
+    torch.cuda.synchronize(dev)
+    t = time.perf_counter() - t
+    groups = [g[0] for g in eng._groups(db)] or [""]
+    return {"structures": len(sts), "k_point_solves": int(plan.nk.sum()), "max_n": int(plan.max_n),
+            "hs_bytes": 2 * 16 * int(plan.hs_total), "launches_per_execute": (eng.launches - l0) // max(args.steps, 1),
+            "eigensolver_launches_per_execute": len(groups), "eigensolver_groups": [str(g) for g in groups],
+            "ms_per_execute": 1e3 * t / max(args.steps, 1)}
+
+
+def run_serving_load(dev, n_requests=2000, rate=20.0, capacity=None, chunk=125):
+    """The serving stream under load: ``n_requests`` Poisson arrivals at ``rate`` per second on a fresh
+    server.  The request set is ``synthetic.serving_requests(n_requests, chunk=chunk)`` (chunk i of
+    ``chunk`` structures from seed 1000 + i, one seeded shuffle), generated on the host cores before
+    the stream starts; ``capacity`` (structures/s, from the all-at-once leg) gives the load fraction."""
+    from slakonet_gb300 import model as M, serving as SV, synthetic as syn
+    t0 = time.perf_counter()
+    sts = syn.serving_requests(n_requests, processes=min(16, os.cpu_count() or 1), chunk=chunk)
+    gen_s = time.perf_counter() - t0
+    sd = syn.default_shell_dict()
+    zs = list(range(1, 66))
+    model = M.MultiElementSkfParameterOptimizer.from_tables(syn.make_tables(zs, sd, seed=SEED))
+    server = SV.Server(model, sd, dev, species=zs, n_workers=3)
+    SV.poisson_stream(server, sts[:8], rate=1000.0, seed=1)          # warm-up
+    lat, wall, res = SV.poisson_stream(server, sts, rate=rate, seed=4)
+    batches = server.batches
+    server.close()
+    nk = [len(st["kpoints"]) for st in sts]
+    pct = {f"p{q}_ms": 1e3 * float(np.percentile(lat, q)) for q in (50, 90, 99)}
+    return {"requests": n_requests, "rate_per_s": rate, **pct,
+            "p999_ms": 1e3 * float(np.percentile(lat, 99.9)), "max_ms": 1e3 * float(lat.max()),
+            "structures_per_s": len(lat) / wall, "k_point_solves_per_s": sum(nk) / wall,
+            "load_fraction_of_capacity": None if not capacity else rate / capacity,
+            "batches": batches, "rejected": sum(1 for r in res if "error" in r), "wall_s": wall,
+            "atoms_total": int(sum(len(st["numbers"]) for st in sts)), "k_points_total": int(sum(nk)),
+            "max_atoms": int(max(len(st["numbers"]) for st in sts)), "generation_s": gen_s,
+            "request_set": f"synthetic.serving_requests({n_requests}, chunk={chunk}): chunks of {chunk} structures, "
+                           "chunk i from seed 1000 + i, one seeded shuffle"}
+
+
 def run_large_structure(dev):
     """1000-atom Ga/As zincblende supercell (5x5x5 conventional cells, a = 5.65 A, 0.05 A jitter),
     spd on both species (n = 9000), Gamma plus the 7 other points of the 2x2x2 Gamma-centred grid:
-    the whole path once, each k-point on a 16-CTA cluster eigensolver."""
+    the whole path once, the eigensolve on the device-wide path."""
     import torch
     from slakonet_gb300 import engine as E, synthetic as syn
     st = syn.zincblende_supercell()
@@ -662,14 +728,16 @@ def run_large_structure(dev):
     for name, a, b in eng.event_log:
         phases[name] = phases.get(name, 0.0) + a.elapsed_time(b) * 1e-3
     n = int(plan.max_n)
-    flops = 32.0 / 3.0 * n ** 3 * len(plan.prob_n)
+    real = plan.prob_real if plan.prob_real is not None else np.zeros(len(plan.prob_n), dtype=bool)
+    flops = float(np.sum(np.where(real, 8.0 / 3.0, 32.0 / 3.0) * plan.prob_n.astype(np.float64) ** 3))
     eig_s = phases.get("eigensolve", wall)
     return {"atoms": len(st["numbers"]), "n": n, "k_points": len(plan.prob_n),
             "eig_status_ok": int((res.eig_status == 0).sum()), "wall_s": wall,
             "phase_s": {k: round(v, 4) for k, v in phases.items()},
             "eigensolve_tflops": flops / eig_s * 1e-12, "gap_eV": float(res.stats[0, E.STAT["gap_ev"]]),
-            "note": "k-points on the cluster eigensolver (skn_eigh_gen_large), one cluster of "
-                    f"{E.cluster_for(n)} CTAs per k-point"}
+            "real_k_points": int(real.sum()), "fp64_flops": flops,
+            "note": "all k-points on the device-wide eigensolver (skn_eigh_gen_wide), real arithmetic for the "
+                    "k-points with 2k integer; FP64 count 8/3 n^3 per real and 32/3 n^3 per complex k-point"}
 
 
 REF_GPU_STRIDE = 32       # reference GPU path: every 32nd structure by size (8 of the 256)
@@ -898,12 +966,20 @@ def main():
     ap.add_argument("--serving-sequential", type=int, default=40,
                     help="requests timed one at a time for the sequential baseline (0 skips it)")
     ap.add_argument("--no-serving-capacity", action="store_true", help="skip the all-at-once capacity leg")
+    ap.add_argument("--serving-load-requests", type=int, default=2000,
+                    help="requests in the serving stream under load (0 skips that leg)")
+    ap.add_argument("--serving-load-rate", type=float, default=20.0,
+                    help="Poisson arrival rate of the serving stream under load (1/s)")
     ap.add_argument("--serving-only", action="store_true",
                     help="run only the serving measurement (one GPU) and print its JSON line with clocks")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip timing the reference package (baseline/_ref) per structure on the GPU, and its "
                          "autograd training step")
     ap.add_argument("--reference-gpu-worker", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--path-only", action="store_true",
+                    help="profiling mode: the path alone on default launch shapes, warm-up then --steps executions")
+    ap.add_argument("--sample-stride", type=int, default=0,
+                    help="with --path-only: every K-th structure by size (16: the CPU-baseline sample)")
     ap.add_argument("--large-structure", action="store_true",
                     help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
     args = ap.parse_args()
@@ -911,6 +987,9 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.reference_gpu_worker:
         reference_gpu_worker(args)
+        return
+    if args.path_only:
+        print(json.dumps(run_path_only(args)))
         return
     if args.impl == "reference":
         if rank == 0:
@@ -922,6 +1001,9 @@ def main():
         with ClockSampler(0) as clk:
             out = run_serving(dev, args.serving_requests, args.serving_rate, args.serving_sequential,
                               not args.no_serving_capacity, args.serving_file)
+            if args.serving_load_requests > 0:
+                cap = (out.get("capacity") or {}).get("structures_per_s")
+                out["serving_load"] = run_serving_load(dev, args.serving_load_requests, args.serving_load_rate, cap)
         out["clocks"] = clk.summary()
         print(json.dumps(out))
         return
@@ -939,6 +1021,10 @@ def main():
             log("serving")
             out["serving"] = run_serving(dev, args.serving_requests, args.serving_rate, args.serving_sequential,
                                          not args.no_serving_capacity, args.serving_file)
+            if args.serving_load_requests > 0:
+                log("serving under load")
+                cap = (out["serving"].get("capacity") or {}).get("structures_per_s")
+                out["serving_load"] = run_serving_load(dev, args.serving_load_requests, args.serving_load_rate, cap)
         if world == 1 and args.large_structure:
             import torch
             log("large structure")

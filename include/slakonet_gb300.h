@@ -133,6 +133,29 @@ int skn_bloch(int n_prob, const int32_t* prob_struct, const int32_t* prob_k, con
               int max_n, double* H, double* S, cudaStream_t stream);
 
 /*
+ * The same Bloch sums organised by atom pair: a warp per (ordered atom pair,
+ * chunk of 16 k-points), its lanes over (k-point, block element), so warps
+ * stay full when blocks are small (1x1, 1x4, 4x4 orbitals) and a small cell's
+ * many k-points spread over many warps.  Values are bitwise those of
+ * skn_bloch.  Replaces the same reference code as skn_bloch.
+ *   n_struct               structures
+ *   n_units, unit_base[n_struct]   work units: structure s owns N_s^2 * ceil(nk_s / 16)
+ *                          of them, numbered from unit_base[s] (exclusive prefix sum)
+ *   k_ptr[n_struct+1]      problem index of each structure's first k-point (problems
+ *                          of a structure are consecutive, k-point order)
+ *   lower                  1: write only the entries on or below the diagonal (what the
+ *                          eigensolvers read; the strict upper triangle is left as it
+ *                          was), 0: the full matrices
+ * Other arguments as skn_bloch.
+ */
+int skn_bloch_pairs(int n_struct, int64_t n_units, const int64_t* unit_base, const int32_t* k_ptr,
+                    const int64_t* hs_off, const int32_t* atom_ptr, const int32_t* orb_ptr,
+                    const int32_t* atom_orb_off, const int32_t* atom_norb, const int64_t* pair_base,
+                    const int64_t* pair_ptr, const int32_t* bond_img, const int64_t* bond_blk, const double* blk_H,
+                    const double* blk_S, const int32_t* image_range, const int64_t* phase_base, const double* phases,
+                    const double* onsite_H, int lower, double* H, double* S, cudaStream_t stream);
+
+/*
  * Batched generalized Hermitian eigenvalues H x = e S x, one problem per
  * (structure, k).  Cholesky S = L L^H, reduction C = L^-1 H L^-H,
  * Householder tridiagonalisation, Sturm bisection; FP64 throughout.

@@ -40,6 +40,7 @@ SIGNATURES = {
     "skn_image_phases": [I32, P, P, P, P, P, P],
     "skn_sk_blocks": [I64, P, P, P, P, P, P, I32, P, P, P, P, P, P, P, P, P, P, P, P, P],
     "skn_bloch": [I32, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, I32, P, P, P],
+    "skn_bloch_pairs": [I32, I64, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, I32, P, P, P],
     "skn_eigh_gen_batched": [I32, P, P, P, P, P, P, P, P, P, I32, P],
     "skn_eigh_gen_batched_real": [I32, P, P, P, P, P, P, P, P, P, I32, P],
     "skn_fermi_gap": [I32, P, P, P, P, P, P, P, F64, F64, I32, P, P, P, P],

@@ -276,6 +276,101 @@ __global__ void __launch_bounds__(NT) k_dos(const int64_t* __restrict__ eig_off,
   dos[(int64_t)s * npts + i] = acc;
 }
 
+// The windowed DOS with fewer exponentials.  A thread owns DG consecutive grid points and an eighth of
+// the k-points (k = kg, kg + 8, ...).  Along the grid a Gaussian obeys g(x + D) = g(x) f(x) and
+// f(x + D) = f(x) r, with t = (x - e) / sigma, d = D / sigma, f = exp(-(t d + d^2 / 2)) and
+// r = exp(-d^2); so a band costs two exponentials at the first grid point inside its window and two
+// multiplications per further point, instead of one exponential per point.  A point takes a band
+// exactly when k_dos would (the same window test on the same values); the recurrence starts inside the
+// window (|t| <= window), so it neither underflows nor loses the points it serves.  The eight k-point
+// groups are added in a fixed order, so the result depends on the structure alone.
+constexpr int DG = 8;                  // grid points per thread
+constexpr int DKG = 8;                 // k-point groups per chunk of grid points
+constexpr int DCH = NT / DKG;          // chunks per CTA
+
+__global__ void __launch_bounds__(NT) k_dos_win(const int64_t* __restrict__ eig_off, const int32_t* __restrict__ nkv,
+                                                const int32_t* __restrict__ nbv, const int64_t* __restrict__ kw_off,
+                                                const double* __restrict__ kweights, const double* __restrict__ eigall,
+                                                const double* __restrict__ muv, double e_lo, double e_hi, int npts,
+                                                double sigma, double window, double* __restrict__ grid,
+                                                double* __restrict__ dos) {
+  __shared__ double part[DKG][DCH][DG];
+  const int s = blockIdx.y;
+  const int kg = threadIdx.x / DCH, cl = threadIdx.x % DCH;
+  const int i0 = (blockIdx.x * DCH + cl) * DG;
+  const int cnt = max(0, min(DG, npts - i0));
+  double x[DG], acc[DG];
+#pragma unroll
+  for (int j = 0; j < DG; ++j) {
+    x[j] = lin_grid(e_lo, e_hi, npts, min(i0 + j, npts - 1));
+    acc[j] = 0.0;
+  }
+  if (s == 0 && kg == 0) {
+#pragma unroll
+    for (int j = 0; j < DG; ++j)
+      if (j < cnt) grid[i0 + j] = x[j];
+  }
+  const int nk = nkv[s], nb = nbv[s];
+  const double* E = eigall + eig_off[s];
+  const double* w = kweights + kw_off[s];
+  const double mu = muv[s];
+  const double inv_sigma = 1.0 / sigma;
+  const double inv_norm = 1.0 / (sigma * sqrt(2.0 * 3.141592653589793));
+  const double d = (npts > 1 ? (e_hi - e_lo) / (double)(npts - 1) : 0.0) * inv_sigma;
+  const double r = exp(-d * d);
+  const bool nan_mu = !(mu == mu);
+  if (cnt > 0 && !nan_mu) {
+    const double lo0 = x[0] - window * sigma;
+    const double hi_last = lin_grid(e_lo, e_hi, npts, i0 + cnt - 1) + window * sigma;   // the chunk's last point
+    for (int k = kg; k < nk; k += DKG) {
+      const double* Ek = E + (int64_t)k * nb;
+      int a = 0, b = nb;                       // first band with (e - mu) H2E >= the first point's window
+      while (a < b) {
+        const int m = (a + b) >> 1;
+        if ((Ek[m] - mu) * H2E < lo0) a = m + 1; else b = m;
+      }
+      double sk[DG];
+#pragma unroll
+      for (int j = 0; j < DG; ++j) sk[j] = 0.0;
+      for (int bb = a; bb < nb; ++bb) {
+        const double ev = (Ek[bb] - mu) * H2E;
+        if (ev > hi_last) break;
+        bool started = false;
+        double g = 0.0, f = 0.0;
+#pragma unroll
+        for (int j = 0; j < DG; ++j) {
+          if (j < cnt && ev >= x[j] - window * sigma && ev <= x[j] + window * sigma) {
+            if (!started) {
+              const double t = (x[j] - ev) * inv_sigma;
+              g = exp(-0.5 * (t * t));
+              f = exp(-fma(t, d, 0.5 * d * d));
+              started = true;
+            }
+            sk[j] += g * inv_norm;
+          }
+          if (started) {
+            g *= f;
+            f *= r;
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < DG; ++j) acc[j] = fma(w[k], sk[j], acc[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < DG; ++j) part[kg][cl][j] = acc[j];
+  __syncthreads();
+  if (kg == 0) {
+    for (int j = 0; j < cnt; ++j) {
+      double v = part[0][cl][j];
+#pragma unroll
+      for (int q = 1; q < DKG; ++q) v += part[q][cl][j];
+      dos[(int64_t)s * npts + i0 + j] = nan_mu ? qnan() : v;
+    }
+  }
+}
+
 // dos_at_fermi (grid point closest to 0), gap centre (DOS minimum within |E| < 2 eV)
 // and trapezoid integral, as get_properties_dict (slakonet/main.py:1766-1782).
 __global__ void __launch_bounds__(NT) k_dos_stats(const double* __restrict__ grid, const double* __restrict__ dos,
@@ -327,9 +422,15 @@ extern "C" int skn_dos(int n_struct, const int64_t* eig_off, const int32_t* nk, 
   if (n_struct == 0) return SKN_OK;
   if (!eig_off || !nk || !nb || !kw_off || !kweights || !eig || !mu || !grid || !dos || !stats) return SKN_ERR_ARG;
   if (n_struct > 65535) return SKN_ERR_CAPACITY;
-  dim3 g((npts + NT - 1) / NT, n_struct);
-  k_dos<<<g, NT, 0, stream>>>(eig_off, nk, nb, kw_off, kweights, eig, mu, e_lo, e_hi, npts, sigma, window_sigmas,
-                              grid, dos);
+  if (window_sigmas > 0.0) {
+    dim3 g((npts + DCH * DG - 1) / (DCH * DG), n_struct);
+    k_dos_win<<<g, NT, 0, stream>>>(eig_off, nk, nb, kw_off, kweights, eig, mu, e_lo, e_hi, npts, sigma,
+                                    window_sigmas, grid, dos);
+  } else {
+    dim3 g((npts + NT - 1) / NT, n_struct);
+    k_dos<<<g, NT, 0, stream>>>(eig_off, nk, nb, kw_off, kweights, eig, mu, e_lo, e_hi, npts, sigma, window_sigmas,
+                                grid, dos);
+  }
   if (cudaPeekAtLastError() != cudaSuccess) return SKN_ERR_CUDA;
   k_dos_stats<<<n_struct, NT, 0, stream>>>(grid, dos, npts, stats);
   return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;

@@ -401,6 +401,9 @@ class BatchResult:
         return self.eig[o: o + int(p.nk[s]) * int(p.nb[s])].view(int(p.nk[s]), int(p.nb[s]))
 
 
+BLOCH_KCHUNK = 16          # k-points per work unit of skn_bloch_pairs (csrc/bloch.cu)
+
+
 class DeviceBatch:
     """A planned batch with its descriptor arrays resident on the device."""
 
@@ -433,6 +436,11 @@ class DeviceBatch:
         self.kwoff = _i64(plan.kw_off, dev)
         self.kw = _f64(plan.kweights, dev)
         self.ne = _f64(plan.nelec, dev)
+        # work units of the Bloch-sum kernel: N_s^2 atom pairs x ceil(nk_s / BLOCH_KCHUNK) k-chunks per structure
+        units = np.diff(plan.atom_ptr).astype(np.int64) ** 2 * ((plan.nk.astype(np.int64) + BLOCH_KCHUNK - 1)
+                                                                 // BLOCH_KCHUNK)
+        self.bloch_units = int(units.sum())
+        self.bloch_unit_base = _i64(np.concatenate([[0], np.cumsum(units)[:-1]]) if len(units) else np.zeros(1), dev)
 
     def h2d_bytes(self) -> int:
         return sum(int(v.numel() * v.element_size()) for v in vars(self).values() if isinstance(v, torch.Tensor))
@@ -440,7 +448,7 @@ class DeviceBatch:
 
 # kernels each ABI call launches (for the launch count the bench reports)
 KERNELS_PER_CALL = {"skn_bond_counts": 1, "skn_bond_fill": 1, "skn_image_phases": 1, "skn_sk_blocks": 1,
-                    "skn_bloch": 1, "skn_eigh_gen_batched": 1, "skn_eigh_gen_vectors": 2, "skn_fermi_gap": 1,
+                    "skn_bloch": 1, "skn_bloch_pairs": 1, "skn_eigh_gen_batched": 1, "skn_eigh_gen_vectors": 2, "skn_fermi_gap": 1,
                     "skn_dos": 2, "skn_eigh_gen_large": 1, "skn_eigh_gen_vectors_noalloc": 2}
 
 def wide_launches(n: int, nb: int = 32, ts: int = 64) -> int:
@@ -513,7 +521,7 @@ class Engine:
 
     def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None,
                  tuning=None, large_threshold: Optional[int] = 1024, large_cluster: Optional[int] = None,
-                 real_path: bool = True, wide_threshold: Optional[int] = None):
+                 real_path: bool = True, wide_threshold: Optional[int] = 1024):
         _dev(tables.device)
         self.tables = tables
         self.tuning = tuning          # autotune.Tuning: eigensolver launch shape per problem-size bucket
@@ -521,7 +529,8 @@ class Engine:
         # see route_large (large_cluster None: cluster_for(n))
         self.large_threshold = large_threshold
         self.large_cluster = large_cluster
-        # problems above wide_threshold orbitals run on the device-wide eigensolver instead (route_wide)
+        # problems above wide_threshold orbitals run on the device-wide eigensolver instead (route_wide):
+        # measured on GB300 it is 4.6x the 4-CTA cluster at n = 1024 and 6-7x at n = 2048-4096
         self.wide_threshold = wide_threshold
         # values-only solves of problems with exactly real H(k), S(k) use the real-arithmetic
         # kernel (skn_eigh_gen_batched_real): same numbers, a quarter of the FP64 work
@@ -631,10 +640,12 @@ class Engine:
         n_prob = len(plan.prob_n)
         Hk = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
         Sk = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
-        self._call("skn_bloch", n_prob, ptr(db.ps), ptr(db.pk), ptr(db.hs_off), ptr(db.atom_ptr), ptr(db.orb_ptr),
-                   ptr(db.orb_atom), ptr(db.aoff), ptr(db.norb), ptr(db.pair_base), ptr(d_pair_ptr), ptr(bond_img),
+        # the eigensolvers read only the lower triangles; full matrices only when they are returned
+        self._call("skn_bloch_pairs", S, db.bloch_units, ptr(db.bloch_unit_base), ptr(db.kptr), ptr(db.hs_off),
+                   ptr(db.atom_ptr),
+                   ptr(db.orb_ptr), ptr(db.aoff), ptr(db.norb), ptr(db.pair_base), ptr(d_pair_ptr), ptr(bond_img),
                    ptr(bond_blk), ptr(blk_H), ptr(blk_S), ptr(db.rng), ptr(db.phb), ptr(phases), ptr(db.onsite),
-                   plan.max_n, ptr(Hk), ptr(Sk), stream)
+                   0 if (keep_hs or hs_only) else 1, ptr(Hk), ptr(Sk), stream)
         self._status = status
         hs_copy = (Hk.clone(), Sk.clone()) if keep_hs else (None, None)
         if hs_only:

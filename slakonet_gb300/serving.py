@@ -15,9 +15,9 @@ batch ends only when its largest eigensolve ends.  So requests are sorted
 into two lanes by orbital count (``large_orbitals``).  ``small_workers`` of
 the workers take small requests only; the others take large requests first
 and small ones when no large one waits.  Within a lane a worker takes the
-cheapest requests first (n^3 x k-points), and large problems run on the
-cluster eigensolver from ``large_threshold`` orbitals up, which shortens
-the longest eigensolve of a batch.
+cheapest requests first (n^3 x k-points), and problems above
+``wide_threshold`` orbitals run on the device-wide eigensolver (every SM on
+one structure's k-points), which shortens the longest eigensolve of a batch.
 
 The reference serves one structure per call (slakonet/optim.py:949-1075 via
 predict_slakonet.py); there is no queue, batch or stream there.
@@ -86,7 +86,8 @@ class Server:
                  n_workers: int = 2, max_batch_problems: int = 8192, dos_range=(-20.0, 10.0),
                  dos_points: int = 1000, dos_sigma: float = 0.1, dos_window: float = 9.0,
                  executor: Optional[Callable] = None, large_orbitals: Optional[int] = 256,
-                 small_workers: Optional[int] = None, large_threshold: Optional[int] = 512):
+                 small_workers: Optional[int] = None, large_threshold: Optional[int] = 512,
+                 wide_threshold: Optional[int] = 512):
         self.model = model
         self.sd = shell_dict
         self.device = torch.device(device)
@@ -102,6 +103,7 @@ class Server:
             small_workers = n_workers - 1 if n_workers >= 2 else 0
         self.small_workers = max(0, min(int(small_workers), n_workers - 1))
         self.large_threshold = large_threshold
+        self.wide_threshold = wide_threshold
         if mem_budget_bytes is None:
             free, _ = torch.cuda.mem_get_info(self.device)
             mem_budget_bytes = int(0.6 * free)
@@ -219,7 +221,8 @@ class Server:
 
     def _execute(self, structures, stream):
         with torch.cuda.stream(stream):
-            eng = E.Engine(self.tables, stream=stream, large_threshold=self.large_threshold)
+            eng = E.Engine(self.tables, stream=stream, large_threshold=self.large_threshold,
+                           wide_threshold=self.wide_threshold)
             plan = E.plan_batch(structures, self.tables)
             db = E.DeviceBatch(plan, self.device)
             res = eng.execute(db, **self.dos)

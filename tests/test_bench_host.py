@@ -69,16 +69,6 @@ def test_reference_arm_other_ranks_exit_without_work():
     assert r.stdout.strip() == ""
 
 
-def test_hbm_context_against_measured_peak(tmp_path):
-    bench = _bench()
-    peaks = tmp_path / "peaks.json"
-    peaks.write_text(json.dumps({"hbm_gbs": 6000.0}))
-    h = bench.hbm_context(1.5e12, 1.0, str(peaks))
-    assert h["achieved_gbs"] == 1500.0 and h["peak_gbs"] == 6000.0 and h["frac"] == 0.25
-    assert bench.hbm_context(None, 1.0, str(peaks)) is None
-    assert bench.hbm_context(1.5e12, 1.0, str(tmp_path / "absent.json")) is None
-
-
 def test_bloch_roofline_counts_h_and_s_writes(tmp_path):
     bench = _bench()
     peaks = tmp_path / "peaks.json"

@@ -41,11 +41,17 @@ def test_gaas_1000_atoms_n9000_eight_kpoints():
     plan = E.plan_batch([st], ts)
     assert len(st["numbers"]) == 1000 and int(plan.max_n) == 9000 and len(plan.prob_n) == 8
     eng = E.Engine(ts)
+    eng.event_log = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     res = eng.run(plan, dos_range=(-20.0, 10.0), dos_points=1000, dos_window=9.0, keep_hs=True)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    eig_s = sum(a.elapsed_time(b) for name, a, b in eng.event_log if name == "eigensolve") * 1e-3
+    real = plan.prob_real if plan.prob_real is not None else np.zeros(8, dtype=bool)
+    flops = float(np.sum(np.where(real, 8.0 / 3.0, 32.0 / 3.0) * plan.prob_n.astype(np.float64) ** 3))
+    print(f"eigensolve: {eig_s:.2f} s, {flops / eig_s * 1e-12:.3f} TFLOP/s FP64 "
+          f"({int(real.sum())} of 8 k-points real; 8/3 n^3 per real, 32/3 n^3 per complex k-point)")
     assert (res.eig_status.cpu().numpy() == 0).all()
     n = 9000
     eig = res.eigenvalues(0)                       # [8, n] Hartree, ascending
