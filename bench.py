@@ -674,6 +674,52 @@ def run_path_only(args):
             "ms_per_execute": 1e3 * t / max(args.steps, 1)}
 
 
+def run_wide_case(spec, steps=1, warmup=1, seed=0):
+    """The device-wide eigensolver alone on ``count`` seeded random Hermitian-definite problems of ``n``
+    orbitals (spec "n:count"), as one group: ``warmup`` untimed then ``steps`` timed calls, each on fresh
+    copies of H and S (the solver works in place).  For profiling and for the rate at a given size."""
+    import ctypes
+    import torch
+    from slakonet_gb300 import _lib, engine as E
+    import __graft_entry__ as ge
+    ge.build()
+    n, count = (int(x) for x in spec.split(":"))
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    X = torch.randn(count, n, n, dtype=torch.complex128, device=dev, generator=g)
+    H0 = ((X + X.mH) / 2).transpose(1, 2).contiguous()
+    Y = torch.randn(count, n, n, dtype=torch.complex128, device=dev, generator=g)
+    S0 = (torch.eye(n, dtype=torch.complex128, device=dev) + (Y + Y.mH) * (0.05 / n ** 0.5)).transpose(1, 2).contiguous()
+    del X, Y
+    nv = torch.full((count,), n, dtype=torch.int32, device=dev)
+    off = torch.arange(count, dtype=torch.int64, device=dev) * n * n
+    eo = torch.arange(count, dtype=torch.int64, device=dev) * n
+    prob = torch.arange(count, dtype=torch.int32, device=dev)
+    eig = torch.empty(count * n, dtype=torch.float64, device=dev)
+    st = torch.empty(count, dtype=torch.int32, device=dev)
+    need = ctypes.c_int64(0)
+    _lib.call("skn_eigh_wide_scratch_bytes", count, n, ctypes.addressof(need))
+    scratch = torch.empty(need.value // 8, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    times = []
+    for i in range(warmup + steps):
+        H = torch.view_as_real(H0.clone()).reshape(-1)
+        S = torch.view_as_real(S0.clone()).reshape(-1)
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        _lib.call("skn_eigh_gen_wide", count, n, _lib.ptr(prob), _lib.ptr(nv), _lib.ptr(off), _lib.ptr(eo),
+                  _lib.ptr(H), _lib.ptr(S), _lib.ptr(eig), _lib.ptr(st), _lib.ptr(scratch), need.value, 0, stream)
+        b.record()
+        torch.cuda.synchronize(dev)
+        if i >= warmup:
+            times.append(a.elapsed_time(b) * 1e-3)
+        del H, S
+    t = min(times)
+    return {"n": n, "problems": count, "seconds": t, "tflops": 32.0 / 3.0 * n ** 3 * count / t / 1e12,
+            "launches_per_call": E.wide_launches(n), "status_ok": int((st == 0).sum())}
+
+
 def run_serving_load(dev, n_requests=2000, rate=20.0, capacity=None, chunk=125):
     """The serving stream under load: ``n_requests`` Poisson arrivals at ``rate`` per second on a fresh
     server.  The request set is ``synthetic.serving_requests(n_requests, chunk=chunk)`` (chunk i of
@@ -980,6 +1026,8 @@ def main():
                     help="profiling mode: the path alone on default launch shapes, warm-up then --steps executions")
     ap.add_argument("--sample-stride", type=int, default=0,
                     help="with --path-only: every K-th structure by size (16: the CPU-baseline sample)")
+    ap.add_argument("--wide-case", default=None, metavar="N:COUNT",
+                    help="time the device-wide eigensolver alone on COUNT random problems of N orbitals")
     ap.add_argument("--large-structure", action="store_true",
                     help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
     args = ap.parse_args()
@@ -990,6 +1038,9 @@ def main():
         return
     if args.path_only:
         print(json.dumps(run_path_only(args)))
+        return
+    if args.wide_case:
+        print(json.dumps(run_wide_case(args.wide_case, args.steps, args.warmup)))
         return
     if args.impl == "reference":
         if rank == 0:

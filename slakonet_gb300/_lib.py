@@ -63,7 +63,7 @@ SIGNATURES = {
     "skn_dos_backward": [I32, P, P, P, P, P, P, P, F64, F64, I32, F64, F64, P, P, I32, P],
     "skn_atom_pdos": [I32, I32, I32, P, P, P, I32, F64, F64, F64, I32, F64, F64, P, P, P, P],
 }
-for _sfx in ("_t64", "_t256", "_blk", "_blk256"):
+for _sfx in ("_t32", "_t64", "_t256", "_blk"):
     SIGNATURES["skn_eigh_gen_batched" + _sfx] = SIGNATURES["skn_eigh_gen_batched"]
     SIGNATURES["skn_eigh_gen_batched_real" + _sfx] = SIGNATURES["skn_eigh_gen_batched"]
     SIGNATURES["skn_eigh_gen_vectors" + _sfx] = SIGNATURES["skn_eigh_gen_vectors"]

@@ -24,8 +24,8 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxe
 # Extra launch shapes of the eigensolver, exported with a suffix and chosen per problem-size
 # bucket by slakonet_gb300.autotune: (suffix, threads per CTA, CTAs per SM, unroll, shared-memory staging n,
 # blocked Cholesky and reduction).
-EIG_SHAPES = [("_t64", 64, 8, 2, 16, 0), ("_t256", 256, 3, 2, 32, 0), ("_blk", 128, 3, 2, 24, 1),
-              ("_blk256", 256, 2, 2, 24, 1)]
+EIG_SHAPES = [("_t32", 32, 16, 2, 16, 0), ("_t64", 64, 8, 2, 16, 0), ("_t256", 256, 3, 2, 32, 0),
+              ("_blk", 128, 3, 2, 24, 1)]
 
 
 def nvcc() -> str:

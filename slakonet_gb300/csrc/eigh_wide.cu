@@ -36,7 +36,7 @@ namespace {
 constexpr int NB = 32;                 // panel width
 constexpr int TS = 64;                 // tile edge of the product kernels
 constexpr int KC = 16;                 // panel columns staged per pass of the tile kernels
-constexpr int RC = 256;                // rows per CTA of the row-parallel kernels
+constexpr int RC = 64;                 // rows per CTA of the row-parallel kernels (many CTAs at mid sizes)
 constexpr int WIDE_MAX_N = 32768;
 constexpr int TLD = TS + 1;            // leading dimension of the staged hemv tile
 
@@ -179,6 +179,20 @@ SKN_DEVINL void tile_ij(int t, int& I, int& J) {
 
 SKN_DEVINL bool live(const Grp& G, int p) { return G.status[p] == SKN_OK; }
 
+// Sum of count values base[c * stride] by one warp: lane l adds c = l, l + 32, ... in order, then a fixed
+// butterfly; every lane returns the same bits, whatever the launch.
+template <bool R>
+SKN_DEVINL double2 warp_chunk_sum(const double2* base, int64_t stride, int count) {
+  const int lane = threadIdx.x & 31;
+  double2 s = make_double2(0.0, 0.0);
+  for (int c = lane; c < count; c += 32) s = zadd<R>(s, zld<R>(base + (int64_t)c * stride));
+  for (int o = 16; o > 0; o >>= 1) {
+    s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+    if constexpr (!R) s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+  }
+  return s;
+}
+
 // ------------------------------------------------------------------ set-up
 // Status per problem (size check) and cleared zero-row flags.
 __global__ void __launch_bounds__(256) k_init(Grp G) {
@@ -307,9 +321,11 @@ __global__ void __launch_bounds__(RC) k_trsm_right(Grp G, int which, int c0, int
 }
 
 // C -= P P^H (MODE 0) or C -= P Q^H + Q P^H (MODE 1) on the lower triangle of the m x m matrix C,
-// P and Q m x K (K <= NB).  One CTA per 64x64 tile; each thread a 4x4 block of accumulators.
-template <bool R, int MODE>
-__global__ void __launch_bounds__(256) k_rank2k(Grp G, Mat Cm, int m, Mat Pm, Mat Qm, int K) {
+// P and Q m x K (K <= NB).  One CTA of (T/4)^2 threads per T x T tile; each thread a 4x4 block of
+// accumulators.  T = 64 for large trailing matrices, 32 when 64-wide tiles would not fill the GPU twice.
+template <bool R, int MODE, int T>
+__global__ void __launch_bounds__((T / 4) * (T / 4)) k_rank2k(Grp G, Mat Cm, int m, Mat Pm, Mat Qm, int K) {
+  constexpr int NTH = (T / 4) * (T / 4);
   const int g = blockIdx.y, p = G.prob[g];
   if (!live(G, p)) return;
   const int n = G.n;
@@ -317,29 +333,29 @@ __global__ void __launch_bounds__(256) k_rank2k(Grp G, Mat Cm, int m, Mat Pm, Ma
   tile_ij(blockIdx.x, I, J);
   extern __shared__ double2 smr[];
   double2* sPI = smr;
-  double2* sQJ = smr + KC * TS;            // MODE 0: P rows of tile J
-  double2* sQI = smr + 2 * KC * TS;
-  double2* sPJ = smr + 3 * KC * TS;
+  double2* sQJ = smr + KC * T;             // MODE 0: P rows of tile J
+  double2* sQI = smr + 2 * KC * T;
+  double2* sPJ = smr + 3 * KC * T;
   double2* C = mat_ptr(G, g, p, Cm);
   const double2* P = mat_ptr(G, g, p, Pm);
   const double2* Q = MODE ? mat_ptr(G, g, p, Qm) : P;
-  const int tid = threadIdx.x, tr = tid & 15, tc = tid >> 4;
+  const int tid = threadIdx.x, tr = tid % (T / 4), tc = tid / (T / 4);
   double2 acc[4][4];
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) acc[u][v] = make_double2(0.0, 0.0);
   for (int k0 = 0; k0 < K; k0 += KC) {
-    for (int e = tid; e < KC * TS; e += 256) {
-      const int r = e & (TS - 1), k = e >> 6, kk = k0 + k;
-      const int gi = I * TS + r, gj = J * TS + r;
+    for (int e = tid; e < KC * T; e += NTH) {
+      const int r = e % T, k = e / T, kk = k0 + k;
+      const int gi = I * T + r, gj = J * T + r;
       const bool okI = gi < m && kk < K, okJ = gj < m && kk < K;
       const double2 z = make_double2(0.0, 0.0);
-      sPI[k * TS + r] = okI ? zld<R>(P + gi + (int64_t)kk * n) : z;
-      sQJ[k * TS + r] = okJ ? zld<R>(Q + gj + (int64_t)kk * n) : z;
+      sPI[k * T + r] = okI ? zld<R>(P + gi + (int64_t)kk * n) : z;
+      sQJ[k * T + r] = okJ ? zld<R>(Q + gj + (int64_t)kk * n) : z;
       if (MODE) {
-        sQI[k * TS + r] = okI ? zld<R>(Q + gi + (int64_t)kk * n) : z;
-        sPJ[k * TS + r] = okJ ? zld<R>(P + gj + (int64_t)kk * n) : z;
+        sQI[k * T + r] = okI ? zld<R>(Q + gi + (int64_t)kk * n) : z;
+        sPJ[k * T + r] = okJ ? zld<R>(P + gj + (int64_t)kk * n) : z;
       }
     }
     __syncthreads();
@@ -347,18 +363,18 @@ __global__ void __launch_bounds__(256) k_rank2k(Grp G, Mat Cm, int m, Mat Pm, Ma
     for (int k = 0; k < KC; ++k) {
       double2 a[4], b[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] = sPI[k * TS + tr * 4 + u];
+      for (int u = 0; u < 4; ++u) a[u] = sPI[k * T + tr * 4 + u];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) b[v] = sQJ[k * TS + tc * 4 + v];
+      for (int v = 0; v < 4; ++v) b[v] = sQJ[k * T + tc * 4 + v];
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = zfma_cj<R>(a[u], b[v], acc[u][v]);
       if (MODE) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) a[u] = sQI[k * TS + tr * 4 + u];
+        for (int u = 0; u < 4; ++u) a[u] = sQI[k * T + tr * 4 + u];
 #pragma unroll
-        for (int v = 0; v < 4; ++v) b[v] = sPJ[k * TS + tc * 4 + v];
+        for (int v = 0; v < 4; ++v) b[v] = sPJ[k * T + tc * 4 + v];
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -369,10 +385,10 @@ __global__ void __launch_bounds__(256) k_rank2k(Grp G, Mat Cm, int m, Mat Pm, Ma
   }
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    const int c = J * TS + tc * 4 + v;
+    const int c = J * T + tc * 4 + v;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int r = I * TS + tr * 4 + u;
+      const int r = I * T + tr * 4 + u;
       if (r < m && c < m && r >= c) {
         double2* t = C + r + (int64_t)c * n;
         double2 val = zsub<R>(zld<R>(t), acc[u][v]);
@@ -524,42 +540,43 @@ __global__ void __launch_bounds__(128) k_trsm_diag(Grp G, int t) {
 }
 
 // Chunk row t's update of the rows below: H[r1:, 0:t*NB] -= L[r1:, t*NB : t*NB+NB] X, X the solved
-// chunk H[t*NB : t*NB+NB, 0:t*NB], r1 = (t+1)*NB.  64x64 output tiles, ntj tile columns.
-template <bool R>
-__global__ void __launch_bounds__(256) k_gemm_nn(Grp G, int t, int ntj) {
+// chunk H[t*NB : t*NB+NB, 0:t*NB], r1 = (t+1)*NB.  T x T output tiles ((T/4)^2 threads), ntj tile columns.
+template <bool R, int T>
+__global__ void __launch_bounds__((T / 4) * (T / 4)) k_gemm_nn(Grp G, int t, int ntj) {
+  constexpr int NTH = (T / 4) * (T / 4);
   const int g = blockIdx.y, p = G.prob[g];
   if (!live(G, p)) return;
   const int n = G.n, r0 = t * NB, r1 = r0 + NB, mr = n - r1, nc = r0;
   const int I = blockIdx.x / ntj, J = blockIdx.x % ntj;
   extern __shared__ double2 smr[];
-  double2* sP = smr;                 // [k][64 rows]
-  double2* sX = smr + KC * TS;       // [k][64 cols]
+  double2* sP = smr;                 // [k][T rows]
+  double2* sX = smr + KC * T;        // [k][T cols]
   const double2* Lp = G.S + G.hs_off[p] + r1 + (int64_t)r0 * n;   // rows r1.., columns r0..r0+NB
   const double2* Xp = G.H + G.hs_off[p] + r0;                      // rows r0..r0+NB, column c at Xp + c*n
   double2* C = G.H + G.hs_off[p] + r1;
-  const int tid = threadIdx.x, tr = tid & 15, tc = tid >> 4;
+  const int tid = threadIdx.x, tr = tid % (T / 4), tc = tid / (T / 4);
   double2 acc[4][4];
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) acc[u][v] = make_double2(0.0, 0.0);
   for (int k0 = 0; k0 < NB; k0 += KC) {
-    for (int e = tid; e < KC * TS; e += 256) {
-      const int r = e & (TS - 1), k = e >> 6;
-      const int gi = I * TS + r;
-      sP[k * TS + r] = gi < mr ? zld<R>(Lp + gi + (int64_t)(k0 + k) * n) : make_double2(0.0, 0.0);
+    for (int e = tid; e < KC * T; e += NTH) {
+      const int r = e % T, k = e / T;
+      const int gi = I * T + r;
+      sP[k * T + r] = gi < mr ? zld<R>(Lp + gi + (int64_t)(k0 + k) * n) : make_double2(0.0, 0.0);
       const int kx = e % KC, cx = e / KC;
-      const int gc = J * TS + cx;
-      sX[kx * TS + cx] = gc < nc ? zld<R>(Xp + (k0 + kx) + (int64_t)gc * n) : make_double2(0.0, 0.0);
+      const int gc = J * T + cx;
+      sX[kx * T + cx] = gc < nc ? zld<R>(Xp + (k0 + kx) + (int64_t)gc * n) : make_double2(0.0, 0.0);
     }
     __syncthreads();
 #pragma unroll 2
     for (int k = 0; k < KC; ++k) {
       double2 a[4], b[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] = sP[k * TS + tr * 4 + u];
+      for (int u = 0; u < 4; ++u) a[u] = sP[k * T + tr * 4 + u];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) b[v] = sX[k * TS + tc * 4 + v];
+      for (int v = 0; v < 4; ++v) b[v] = sX[k * T + tc * 4 + v];
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -569,10 +586,10 @@ __global__ void __launch_bounds__(256) k_gemm_nn(Grp G, int t, int ntj) {
   }
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    const int c = J * TS + tc * 4 + v;
+    const int c = J * T + tc * 4 + v;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int r = I * TS + tr * 4 + u;
+      const int r = I * T + tr * 4 + u;
       if (r < mr && c < nc) {
         double2* q = C + r + (int64_t)c * n;
         zst<R>(q, zsub<R>(zld<R>(q), acc[u][v]));
@@ -634,10 +651,9 @@ __global__ void __launch_bounds__(256) k_tr_reflect(Grp G, int c0, int j) {
   double2* x = A + (k + 1) + (int64_t)k * n;
   __shared__ double2 s_scl;
   __shared__ int s_triv;
+  double xnorm2 = 0.0;
+  if (threadIdx.x < 32) xnorm2 = warp_chunk_sum<true>(w.r1, 1, cdiv_d(M - j, RC)).x;
   if (threadIdx.x == 0) {
-    const int nch = cdiv_d(M - j, RC);
-    double xnorm2 = 0.0;
-    for (int c = 0; c < nch; ++c) xnorm2 += w.r1[c].x;
     const double2 alpha = zld<R>(x);
     double beta, taur, taui;
     double2 scl = make_double2(0.0, 0.0);
@@ -758,7 +774,7 @@ __global__ void __launch_bounds__(256) k_tr_hemv(Grp G, int base, int m) {
 //    W(:, q)^H v and V(:, q)^H v over the chunk for the panel's earlier columns q < j (warp per
 //    product, lanes over rows, fixed reduction tree).
 template <bool R>
-__global__ void __launch_bounds__(RC) k_tr_dots(Grp G, int c0, int j) {
+__global__ void __launch_bounds__(256) k_tr_dots(Grp G, int c0, int j) {
   const int g = blockIdx.y, p = G.prob[g];
   if (!live(G, p)) return;
   const WS w = ws_of(G, g);
@@ -766,22 +782,25 @@ __global__ void __launch_bounds__(RC) k_tr_dots(Grp G, int c0, int j) {
   const int n = G.n, m = n - c0 - j - 1, nt = cdiv_d(m, TS);
   const double2* A = G.H + G.hs_off[p];
   __shared__ double2 vloc[RC];
-  const int i = blockIdx.x * RC + threadIdx.x;
-  if (i < m) {
-    double2 y = zld<R>(w.Yp + i);
-    for (int s = 1; s < nt; ++s) y = zadd<R>(y, zld<R>(w.Yp + (int64_t)s * n + i));
-    zst<R>(w.y + i, y);
-    vloc[threadIdx.x] = zld<R>(w.v + i);
-  } else {
-    vloc[threadIdx.x] = make_double2(0.0, 0.0);
+  if (threadIdx.x < RC) {
+    const int i = blockIdx.x * RC + threadIdx.x;
+    if (i < m) {
+      double2 y = zld<R>(w.Yp + i);
+      for (int s = 1; s < nt; ++s) y = zadd<R>(y, zld<R>(w.Yp + (int64_t)s * n + i));
+      zst<R>(w.y + i, y);
+      vloc[threadIdx.x] = zld<R>(w.v + i);
+    } else {
+      vloc[threadIdx.x] = make_double2(0.0, 0.0);
+    }
   }
   if (j == 0) return;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int row0 = c0 + j + 1 + blockIdx.x * RC;     // global row of the chunk's first row
-  for (int dq = warp; dq < 2 * j; dq += RC / 32) {
+  for (int dq = warp; dq < 2 * j; dq += 8) {
     const double2* src = dq < j ? w.W + (int64_t)dq * n : A + (int64_t)(c0 + dq - j) * n;
     double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
     for (int rr = lane; rr < RC; rr += 32) {
       if (blockIdx.x * RC + rr < m) acc = zfma_cja<R>(zld<R>(src + row0 + rr), vloc[rr], acc);
     }
@@ -810,21 +829,29 @@ __global__ void __launch_bounds__(RC) k_tr_wupd(Grp G, int c0, int j) {
   }
   const double2* A = G.H + G.hs_off[p];
   __shared__ double2 t12[2 * NB];
-  if (threadIdx.x < 2 * j) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int c = 0; c < nch; ++c) s = zadd<R>(s, zld<R>(w.r2 + (int64_t)c * 2 * NB + threadIdx.x));
-    t12[threadIdx.x] = s;                         // [0, j): W^H v, [j, 2j): V^H v
+  for (int dq = threadIdx.x >> 5; dq < 2 * j; dq += RC / 32) {   // [0, j): W^H v, [j, 2j): V^H v
+    const double2 sdq = warp_chunk_sum<R>(w.r2 + dq, 2 * NB, nch);
+    if ((threadIdx.x & 31) == 0) t12[dq] = sdq;
   }
   __syncthreads();
   const double2 tau = w.sc[0];
   double pr = 0.0, pi = 0.0;
   if (i < m) {
-    double2 y0 = zld<R>(w.y + i), y1 = make_double2(0.0, 0.0);
-    for (int q = 0; q < j; ++q) {
+    double2 y0 = zld<R>(w.y + i), y1 = make_double2(0.0, 0.0), y2 = y1, y3 = y1;
+    int q = 0;
+    for (; q + 1 < j; q += 2) {        // two columns per step: four independent chains, four loads ahead
+      const double2 v0 = zld<R>(A + gr + (int64_t)(c0 + q) * n), v1 = zld<R>(A + gr + (int64_t)(c0 + q + 1) * n);
+      const double2 w0 = zld<R>(w.W + (int64_t)q * n + gr), w1 = zld<R>(w.W + (int64_t)(q + 1) * n + gr);
+      y0 = zfms<R>(v0, t12[q], y0);
+      y1 = zfms<R>(w0, t12[j + q], y1);
+      y2 = zfms<R>(v1, t12[q + 1], y2);
+      y3 = zfms<R>(w1, t12[j + q + 1], y3);
+    }
+    if (q < j) {
       y0 = zfms<R>(zld<R>(A + gr + (int64_t)(c0 + q) * n), t12[q], y0);
       y1 = zfms<R>(zld<R>(w.W + (int64_t)q * n + gr), t12[j + q], y1);
     }
-    const double2 wi = zmul<R>(tau, zadd<R>(y0, y1));
+    const double2 wi = zmul<R>(tau, zadd<R>(zadd<R>(y0, y2), zadd<R>(y1, y3)));
     zst<R>(w.W + (int64_t)j * n + gr, wi);
     const double2 vi = zld<R>(w.v + i);
     if constexpr (R) {
@@ -848,11 +875,10 @@ __global__ void __launch_bounds__(RC) k_tr_wfin(Grp G, int c0, int j) {
   if (w.sc[2].x != 0.0) return;
   const int n = G.n, m = n - c0 - j - 1, nch = cdiv_d(m, RC);
   __shared__ double2 s_al;
-  if (threadIdx.x == 0) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int c = 0; c < nch; ++c) s = zadd<R>(s, zld<R>(w.r3 + c));
+  if (threadIdx.x < 32) {
+    const double2 s = warp_chunk_sum<R>(w.r3, 1, nch);
     const double2 tau = w.sc[0];
-    s_al = zmul<R>(make_double2(-0.5 * tau.x, -0.5 * tau.y), s);
+    if (threadIdx.x == 0) s_al = zmul<R>(make_double2(-0.5 * tau.x, -0.5 * tau.y), s);
   }
   __syncthreads();
   const int i = blockIdx.x * RC + threadIdx.x;
@@ -922,29 +948,58 @@ __global__ void __launch_bounds__(128) k_tri_eig(Grp G) {
 }
 
 // ------------------------------------------------------------------ host sequence
-constexpr int SM_R2K = 4 * KC * TS * (int)sizeof(double2);             // 64 KB
-constexpr int SM_HERK = 2 * KC * TS * (int)sizeof(double2);            // 32 KB
-constexpr int SM_GEMM = 2 * KC * TS * (int)sizeof(double2);            // 32 KB
 constexpr int SM_HEMV = (TS * TLD + 2 * TS) * (int)sizeof(double2);    // 67 KB
 static_assert(8 * TS <= TS * TLD, "hemv partials fit in the tile's space");
+constexpr int sm_r2k(int mode, int t) { return (mode ? 4 : 2) * KC * t * (int)sizeof(double2); }   // <= 64 KB
+constexpr int sm_gemm(int t) { return 2 * KC * t * (int)sizeof(double2); }
 
 template <bool R>
 cudaError_t set_attrs() {
-  cudaError_t e = cudaFuncSetAttribute(k_rank2k<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_R2K);
+  cudaError_t e = cudaFuncSetAttribute(k_rank2k<R, 1, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_r2k(1, 64));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tr_hemv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_HEMV);
   return e;
 }
 
-inline unsigned tri_tiles(int m) {
-  const int nt = cdiv(m, TS);
+inline unsigned tri_tiles(int m, int t = TS) {
+  const int nt = cdiv(m, t);
   return (unsigned)(nt * (nt + 1) / 2);
+}
+
+// Tile edge for a product kernel: 64 unless its grid would fill fewer than two waves of the GPU's SMs.
+inline bool small_tiles(int64_t tiles64, int n_prob, int sms) { return tiles64 * n_prob < 2LL * sms; }
+
+template <bool R, int MODE>
+void rank2k(const Grp& G, Mat C, int m, Mat P, Mat Q, int K, int sms, cudaStream_t st) {
+  const unsigned Pn = (unsigned)G.n_prob;
+  if (small_tiles(tri_tiles(m, 64), G.n_prob, sms))
+    k_rank2k<R, MODE, 32><<<dim3(tri_tiles(m, 32), Pn), 64, sm_r2k(MODE, 32), st>>>(G, C, m, P, Q, K);
+  else
+    k_rank2k<R, MODE, 64><<<dim3(tri_tiles(m, 64), Pn), 256, sm_r2k(MODE, 64), st>>>(G, C, m, P, Q, K);
+}
+
+template <bool R>
+void gemm_nn(const Grp& G, int t, int sms, cudaStream_t st) {
+  const int n = G.n;
+  const unsigned Pn = (unsigned)G.n_prob;
+  const int64_t t64 = (int64_t)cdiv(n - (t + 1) * NB, 64) * cdiv(t * NB, 64);
+  if (small_tiles(t64, G.n_prob, sms)) {
+    const int ntj = cdiv(t * NB, 32);
+    k_gemm_nn<R, 32><<<dim3((unsigned)(cdiv(n - (t + 1) * NB, 32) * ntj), Pn), 64, sm_gemm(32), st>>>(G, t, ntj);
+  } else {
+    const int ntj = cdiv(t * NB, 64);
+    k_gemm_nn<R, 64><<<dim3((unsigned)(cdiv(n - (t + 1) * NB, 64) * ntj), Pn), 256, sm_gemm(64), st>>>(G, t, ntj);
+  }
 }
 
 template <bool R>
 void run(const Grp& G, cudaStream_t st) {
   const int n = G.n;
   const unsigned P = (unsigned)G.n_prob;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms < 1) sms = 1;
   k_init<<<dim3(cdiv(2 * n, 256), P), 256, 0, st>>>(G);
   k_zscan<R><<<dim3(cdiv(n, 256), cdiv(n, 256), 2 * P), 256, 0, st>>>(G);
   k_zfix<R><<<dim3(cdiv(n, 256), 2 * P), 256, 0, st>>>(G);
@@ -954,8 +1009,8 @@ void run(const Grp& G, cudaStream_t st) {
     k_potrf<R><<<P, 32, 0, st>>>(G, c0, w);
     if (m > 0) {
       k_trsm_right<R><<<dim3(cdiv(m, RC), P), RC, 0, st>>>(G, 1, c0, m);
-      k_rank2k<R, 0><<<dim3(tri_tiles(m), P), 256, SM_HERK, st>>>(
-          G, Mat{1, (int64_t)(c0 + NB) * (n + 1)}, m, Mat{1, (c0 + NB) + (int64_t)c0 * n}, Mat{1, 0}, NB);
+      rank2k<R, 0>(G, Mat{1, (int64_t)(c0 + NB) * (n + 1)}, m, Mat{1, (c0 + NB) + (int64_t)c0 * n}, Mat{1, 0}, NB,
+                   sms, st);
     }
   }
   // reduction to standard form, the panels' left solves deferred
@@ -965,19 +1020,15 @@ void run(const Grp& G, cudaStream_t st) {
     if (m > 0) {
       k_trsm_right<R><<<dim3(cdiv(m, RC), P), RC, 0, st>>>(G, 0, c0, m);
       k_hemm_half<R><<<dim3(cdiv(m * NB, 256), P), 256, 0, st>>>(G, c0, m);
-      k_rank2k<R, 1><<<dim3(tri_tiles(m), P), 256, SM_R2K, st>>>(
-          G, Mat{0, (int64_t)(c0 + NB) * (n + 1)}, m, Mat{0, (c0 + NB) + (int64_t)c0 * n},
-          Mat{1, (c0 + NB) + (int64_t)c0 * n}, NB);
+      rank2k<R, 1>(G, Mat{0, (int64_t)(c0 + NB) * (n + 1)}, m, Mat{0, (c0 + NB) + (int64_t)c0 * n},
+                   Mat{1, (c0 + NB) + (int64_t)c0 * n}, NB, sms, st);
       k_hemm_half<R><<<dim3(cdiv(m * NB, 256), P), 256, 0, st>>>(G, c0, m);
     }
   }
   const int T = cdiv(n, NB);
   for (int t = 1; t < T; ++t) {
     k_trsm_diag<R><<<dim3(cdiv(t * NB, 128), P), 128, 0, st>>>(G, t);
-    if ((t + 1) * NB < n) {
-      const int nti = cdiv(n - (t + 1) * NB, TS), ntj = cdiv(t * NB, TS);
-      k_gemm_nn<R><<<dim3((unsigned)(nti * ntj), P), 256, SM_GEMM, st>>>(G, t, ntj);
-    }
+    if ((t + 1) * NB < n) gemm_nn<R>(G, t, sms, st);
   }
   // tridiagonalisation
   for (int c0 = 0; c0 < n - 1; c0 += NB) {
@@ -987,14 +1038,14 @@ void run(const Grp& G, cudaStream_t st) {
       k_tr_colupd<R><<<dim3(cdiv(M - j, RC), P), RC, 0, st>>>(G, c0, j);
       k_tr_reflect<R><<<P, 256, 0, st>>>(G, c0, j);
       k_tr_hemv<R><<<dim3(tri_tiles(m), P), 256, SM_HEMV, st>>>(G, c0 + j + 1, m);
-      k_tr_dots<R><<<dim3(cdiv(m, RC), P), RC, 0, st>>>(G, c0, j);
+      k_tr_dots<R><<<dim3(cdiv(m, RC), P), 256, 0, st>>>(G, c0, j);
       k_tr_wupd<R><<<dim3(cdiv(m, RC), P), RC, 0, st>>>(G, c0, j);
       k_tr_wfin<R><<<dim3(cdiv(m, RC), P), RC, 0, st>>>(G, c0, j);
     }
     const int m2 = M - w;
     if (m2 > 0)
-      k_rank2k<R, 1><<<dim3(tri_tiles(m2), P), 256, SM_R2K, st>>>(
-          G, Mat{0, (int64_t)(c0 + w) * (n + 1)}, m2, Mat{0, (c0 + w) + (int64_t)c0 * n}, Mat{2, c0 + w}, w);
+      rank2k<R, 1>(G, Mat{0, (int64_t)(c0 + w) * (n + 1)}, m2, Mat{0, (c0 + w) + (int64_t)c0 * n}, Mat{2, c0 + w}, w,
+                   sms, st);
   }
   k_tri_bounds<R><<<P, 256, 0, st>>>(G);
   k_tri_eig<<<dim3(cdiv(n, 128), P), 128, 0, st>>>(G);

@@ -335,20 +335,27 @@ __global__ void __launch_bounds__(NT) k_dos_win(const int64_t* __restrict__ eig_
       for (int bb = a; bb < nb; ++bb) {
         const double ev = (Ek[bb] - mu) * H2E;
         if (ev > hi_last) break;
-        bool started = false;
-        double g = 0.0, f = 0.0;
+        // the points whose window holds ev form one run [j0, j1] (the grid ascends); the same tests as k_dos
+        int j0 = DG, j1 = -1;
+        double xs = x[0];
 #pragma unroll
         for (int j = 0; j < DG; ++j) {
-          if (j < cnt && ev >= x[j] - window * sigma && ev <= x[j] + window * sigma) {
-            if (!started) {
-              const double t = (x[j] - ev) * inv_sigma;
-              g = exp(-0.5 * (t * t));
-              f = exp(-fma(t, d, 0.5 * d * d));
-              started = true;
-            }
-            sk[j] += g * inv_norm;
+          const bool in = j < cnt && ev >= x[j] - window * sigma && ev <= x[j] + window * sigma;
+          if (in && j0 == DG) {
+            j0 = j;
+            xs = x[j];
           }
-          if (started) {
+          if (in) j1 = j;
+        }
+        if (j1 < 0) continue;
+        // both exponentials at the run's first point, every lane together
+        const double t = (xs - ev) * inv_sigma;
+        double g = exp(-0.5 * (t * t));
+        double f = exp(-fma(t, d, 0.5 * d * d));
+#pragma unroll
+        for (int j = 0; j < DG; ++j) {
+          if (j >= j0 && j <= j1) {
+            sk[j] += g * inv_norm;
             g *= f;
             f *= r;
           }
