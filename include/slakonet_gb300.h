@@ -287,11 +287,14 @@ int skn_eigh_gen_wide(int n_prob, int n, const int32_t* prob, const int32_t* nve
 int skn_eigh_wide_scratch_bytes(int n_prob, int n, int64_t* bytes);
 
 /*
- * The same eigensolver compiled in two more launch shapes: 64 threads per CTA
- * with up to 8 CTAs per SM (suffix _t64), and 256 threads with up to 3 CTAs per
- * SM (suffix _t256).  The unsuffixed entry points use 128 threads and up to 5
- * CTAs per SM.  Contracts are identical.  The project's autotuner
- * (slakonet_gb300/autotune.py) picks a shape per problem-size bucket.
+ * The same eigensolver compiled in more launch shapes: 32 threads per CTA with
+ * up to 16 CTAs per SM (suffix _t32), 64 threads with up to 8 (_t64), 256
+ * threads with up to 3 (_t256), and 128 threads with up to 3 whose Cholesky and
+ * reduction run in 32-column panels (_blk).  The unsuffixed entry points use
+ * 128 threads and up to 5 CTAs per SM.  Contracts are identical.  The project's
+ * autotuner (slakonet_gb300/autotune.py) picks a shape per problem-size bucket.
+ * Each shape exports the four entry points below with its suffix; the _t64 and
+ * _t256 ones are spelled out.
  */
 int skn_eigh_gen_batched_t64(int n_prob, const int32_t* n, const int64_t* hs_off, const int64_t* eig_off,
                              const int32_t* order, double* H, double* S, double* eig, int32_t* status,
