@@ -674,10 +674,11 @@ def run_path_only(args):
             "ms_per_execute": 1e3 * t / max(args.steps, 1)}
 
 
-def run_wide_case(spec, steps=1, warmup=1, seed=0):
+def run_wide_case(spec, steps=1, warmup=1, seed=0, tc=False):
     """The device-wide eigensolver alone on ``count`` seeded random Hermitian-definite problems of ``n``
     orbitals (spec "n:count"), as one group: ``warmup`` untimed then ``steps`` timed calls, each on fresh
-    copies of H and S (the solver works in place).  For profiling and for the rate at a given size."""
+    copies of H and S (the solver works in place).  For profiling and for the rate at a given size; ``tc``
+    runs the rank-2k updates on the tensor cores (skn_eigh_gen_wide_tc)."""
     import ctypes
     import torch
     from slakonet_gb300 import _lib, engine as E
@@ -708,7 +709,8 @@ def run_wide_case(spec, steps=1, warmup=1, seed=0):
         torch.cuda.synchronize(dev)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        _lib.call("skn_eigh_gen_wide", count, n, _lib.ptr(prob), _lib.ptr(nv), _lib.ptr(off), _lib.ptr(eo),
+        _lib.call("skn_eigh_gen_wide_tc" if tc else "skn_eigh_gen_wide", count, n, _lib.ptr(prob), _lib.ptr(nv),
+                  _lib.ptr(off), _lib.ptr(eo),
                   _lib.ptr(H), _lib.ptr(S), _lib.ptr(eig), _lib.ptr(st), _lib.ptr(scratch), need.value, 0, stream)
         b.record()
         torch.cuda.synchronize(dev)
@@ -716,8 +718,9 @@ def run_wide_case(spec, steps=1, warmup=1, seed=0):
             times.append(a.elapsed_time(b) * 1e-3)
         del H, S
     t = min(times)
-    return {"n": n, "problems": count, "seconds": t, "tflops": 32.0 / 3.0 * n ** 3 * count / t / 1e12,
-            "launches_per_call": E.wide_launches(n), "status_ok": int((st == 0).sum())}
+    return {"n": n, "problems": count, "tensor_cores": bool(tc), "seconds": t,
+            "tflops": 32.0 / 3.0 * n ** 3 * count / t / 1e12, "launches_per_call": E.wide_launches(n, tc=tc),
+            "status_ok": int((st == 0).sum())}
 
 
 def run_serving_load(dev, n_requests=2000, rate=20.0, capacity=None, chunk=125):
@@ -1028,6 +1031,8 @@ def main():
                     help="with --path-only: every K-th structure by size (16: the CPU-baseline sample)")
     ap.add_argument("--wide-case", default=None, metavar="N:COUNT",
                     help="time the device-wide eigensolver alone on COUNT random problems of N orbitals")
+    ap.add_argument("--wide-tc", action="store_true",
+                    help="with --wide-case or --large-structure: rank-2k updates on the tensor cores")
     ap.add_argument("--large-structure", action="store_true",
                     help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
     args = ap.parse_args()
@@ -1040,7 +1045,7 @@ def main():
         print(json.dumps(run_path_only(args)))
         return
     if args.wide_case:
-        print(json.dumps(run_wide_case(args.wide_case, args.steps, args.warmup)))
+        print(json.dumps(run_wide_case(args.wide_case, args.steps, args.warmup, tc=args.wide_tc)))
         return
     if args.impl == "reference":
         if rank == 0:

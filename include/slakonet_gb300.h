@@ -285,6 +285,20 @@ int skn_eigh_gen_wide(int n_prob, int n, const int32_t* prob, const int32_t* nve
                       int64_t scratch_bytes, int real, cudaStream_t stream);
 /* Host-side query: bytes of `scratch` skn_eigh_gen_wide needs (written to *bytes). */
 int skn_eigh_wide_scratch_bytes(int n_prob, int n, int64_t* bytes);
+/*
+ * skn_eigh_gen_wide with its rank-2k trailing updates (Cholesky, reduction
+ * and tridiagonalisation panels, trailing matrices of 512 rows and more) on
+ * the bf16 tensor cores (tcgen05, TMEM accumulators), FP64-accurate by
+ * error-free splitting: every row of the update's operands is split into 7
+ * integer slices of 7 bits, slice products of one level accumulate exactly in
+ * FP32, and the levels are combined exactly before one FP64 rounding.  Same
+ * arguments, scratch and contract as skn_eigh_gen_wide; a tensor-core stage
+ * whose completion wait runs out sets the problem's status to SKN_ERR_CUDA.
+ * No reference counterpart beyond the eighb call skn_eigh_gen_wide replaces.
+ */
+int skn_eigh_gen_wide_tc(int n_prob, int n, const int32_t* prob, const int32_t* nvec, const int64_t* hs_off,
+                         const int64_t* eig_off, double* H, double* S, double* eig, int32_t* status, double* scratch,
+                         int64_t scratch_bytes, int real, cudaStream_t stream);
 
 /*
  * The same eigensolver compiled in more launch shapes: 32 threads per CTA with

@@ -57,6 +57,7 @@ SIGNATURES = {
     "skn_eigh_large_scratch_bytes": [I32, I32, I32, P],
     "skn_eigh_gen_wide": [I32, I32, P, P, P, P, P, P, P, P, P, I64, I32, P],
     "skn_eigh_wide_scratch_bytes": [I32, I32, P],
+    "skn_eigh_gen_wide_tc": [I32, I32, P, P, P, P, P, P, P, P, P, I64, I32, P],
     "skn_adj_projectors": [I32, P, P, P, P, P, P, P, P, P, P],
     "skn_adj_bloch": [I64] + [P] * 18 + [P],
     "skn_adj_tables": [I64, P, P, P, P, P, P, I32, P, P, P, P, P, P, P, P, P, P, P, P],

@@ -28,6 +28,8 @@
 // block of complex accumulators fed from shared memory (8 shared loads per 64 FMAs), and the
 // matrix-vector product reads each 64x64 tile once for both of its products.  R = true runs the same
 // code on the real parts only (problems whose H(k), S(k) are exactly real).
+#include <cuda_bf16.h>
+
 #include "skn_common.cuh"
 #include "sturm.cuh"
 
@@ -39,6 +41,7 @@ constexpr int KC = 16;                 // panel columns staged per pass of the t
 constexpr int RC = 64;                 // rows per CTA of the row-parallel kernels (many CTAs at mid sizes)
 constexpr int WIDE_MAX_N = 32768;
 constexpr int TLD = TS + 1;            // leading dimension of the staged hemv tile
+constexpr int TCS = 7;                 // integer slices per operand row in the tensor-core update
 
 SKN_DEVINL int cdiv_d(int a, int b) { return (a + b - 1) / b; }
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
@@ -92,7 +95,7 @@ SKN_DEVINL double2 zconj(double2 a) { return make_double2(a.x, flip_sign(a.y)); 
 // ------------------------------------------------------------------ scratch layout (per problem slot)
 // All offsets in double2 units, each region 256-byte aligned.
 struct Lay {
-  int64_t W, v, y, Yp, r1, r2, r3, sc, d, e2, rd, d32, e232, flg, stride;
+  int64_t W, v, y, Yp, r1, r2, r3, sc, d, e2, rd, d32, e232, flg, tcs, tce, stride;
 };
 __host__ __device__ inline int64_t take(int64_t& o, int64_t cnt) {
   const int64_t r = o;
@@ -117,6 +120,8 @@ __host__ __device__ inline Lay layout(int n) {
   L.d32 = take(o, (n + 3) / 4);
   L.e232 = take(o, (n + 3) / 4);
   L.flg = take(o, (2 * (int64_t)n + 3) / 4);
+  L.tcs = take(o, (int64_t)3 * TCS * n * 128 * 2 / 16);   // bf16 slices of the tensor-core update (A, A', B)
+  L.tce = take(o, ((int64_t)n + 3) / 4);                    // their row exponents
   L.stride = o;
   return L;
 }
@@ -126,6 +131,8 @@ struct WS {
   double *d, *e2, *rd;
   float *d32, *e232;
   int* flg;
+  uint16_t* tcs;   // bf16 slices: [form][TCS][n][KP], form 0 A (A_r), 1 A' (A_i, complex), 2 B
+  int* tce;        // row exponents of the sliced rows
 };
 
 // What every launch needs: the group and its buffers.
@@ -154,6 +161,8 @@ SKN_DEVINL WS ws_of(const Grp& G, int g) {
   w.d32 = reinterpret_cast<float*>(b + L.d32);
   w.e232 = reinterpret_cast<float*>(b + L.e232);
   w.flg = reinterpret_cast<int*>(b + L.flg);
+  w.tcs = reinterpret_cast<uint16_t*>(b + L.tcs);
+  w.tce = reinterpret_cast<int*>(b + L.tce);
   return w;
 }
 
@@ -397,6 +406,285 @@ __global__ void __launch_bounds__((T / 4) * (T / 4)) k_rank2k(Grp G, Mat Cm, int
       }
     }
   }
+}
+
+// ------------------------------------------------------------------ rank-2k on the tensor cores
+// The same update as k_rank2k, C -= P Q^H + Q P^H (MODE 1) or C -= P P^H (MODE 0), computed on the bf16
+// tensor cores by error-free splitting (Ozaki, Ogita and Oishi, Numer. Algorithms 59, 2012).  In real form
+// the complex update is two real products with a 4K-wide inner dimension KP = 128:
+//   C_r -= A B^T,  C_i -= A' B^T,  A = [Pr Pi Qr Qi],  A' = [Pi -Pr Qi -Qr],  B = [Qr Qi Pr Pi]
+// (MODE 0: A = [Pr Pi 0 0], A' = [Pi -Pr 0 0], B = [Pr Pi 0 0]); a real problem needs one product with
+// KP = 64, A = [P Q], B = [Q P] (MODE 0: [P 0], [P 0]).  Every row of A, A' and B holds the same values, so
+// one exponent e_r per row serves all three: x = 2^e_r sum_s d_s 2^(-7(s+1)) with TCS integer digits
+// d_s (rounded to nearest, |d_0| <= 128, later |d_s| <= 64), each exact in bf16.  A slice product is an
+// integer below 2^14 and a K = 128 sum below 2^21, so all slice pairs with the same level s + t (at most
+// TCS = 7 of them) accumulate exactly in one FP32 TMEM accumulator (below 2^24).  The levels are combined
+// exactly in two int64 halves and rounded once to FP64.  With 7 slices of 7 bits the dropped pairs
+// (s + t >= 7) and digits lie near 2^-49 of each row's scale.
+
+SKN_DEVINL uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+// Shared-memory matrix descriptor: no swizzle, K-major core matrices (8 rows x 16 bytes), LBO = 128 bytes
+// between core matrices along K, sbo bytes between 8-row groups.
+SKN_DEVINL uint64_t tc_desc(uint32_t addr, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((128u >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major, M = 128, N = 32.
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(32 >> 3) << 17) |
+                              ((uint32_t)(128 >> 4) << 24);
+
+SKN_DEVINL void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t"
+      "}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(TC_IDESC), "r"(accumulate));
+}
+
+constexpr long long TC_WAIT_LIMIT = 1LL << 26;    // mbarrier polls before giving up
+
+SKN_DEVINL bool tc_wait(uint32_t bar, uint32_t parity) {
+  for (long long it = 0; it < TC_WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t"
+        "}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity));
+    if (done) return true;
+  }
+  return false;
+}
+
+SKN_DEVINL uint16_t bf16_bits(double d) { return __bfloat16_as_ushort(__double2bfloat16(d)); }
+
+// Slices of the m rows of the panel update (one warp per row; lane l holds column l of each K block).
+template <bool R, int MODE>
+__global__ void __launch_bounds__(256) k_r2k_split(Grp G, Mat Pm, Mat Qm, int m, int K) {
+  constexpr int KP = R ? 64 : 128, NSEC = KP / 32;
+  const int g = blockIdx.y, p = G.prob[g];
+  if (!live(G, p)) return;
+  const int n = G.n, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (r >= m) return;
+  const WS w = ws_of(G, g);
+  const double2* P = mat_ptr(G, g, p, Pm);
+  const double2* Q = MODE ? mat_ptr(G, g, p, Qm) : P;
+  // x[0..NSEC): complex [Pr, Pi, Qr, Qi], real [P, Q]; zero beyond K, and the Q part in MODE 0
+  double x[4] = {0.0, 0.0, 0.0, 0.0};
+  if (lane < K) {
+    const double2 pv = zld<R>(P + r + (int64_t)lane * n);
+    const double2 qv = MODE ? zld<R>(Q + r + (int64_t)lane * n) : make_double2(0.0, 0.0);
+    if constexpr (R) {
+      x[0] = pv.x;
+      x[1] = qv.x;
+    } else {
+      x[0] = pv.x;
+      x[1] = pv.y;
+      x[2] = qv.x;
+      x[3] = qv.y;
+    }
+  }
+  double amax = 0.0;
+#pragma unroll
+  for (int i = 0; i < NSEC; ++i) amax = fmax(amax, fabs(x[i]));
+  for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  int ex = 0;
+  if (amax > 0.0) frexp(amax, &ex);                 // amax = f 2^ex, f in [0.5, 1): |x| 2^-ex < 1
+  if (lane == 0) w.tce[r] = ex;
+  double v[4];
+#pragma unroll
+  for (int i = 0; i < NSEC; ++i) v[i] = ldexp(x[i], -ex);   // exact
+  uint16_t* base = w.tcs;
+  for (int sl = 0; sl < TCS; ++sl) {
+    double dgt[4];
+#pragma unroll
+    for (int i = 0; i < NSEC; ++i) {
+      v[i] *= 128.0;                                // exact
+      dgt[i] = rint(v[i]);                          // |dgt| <= 128, then <= 64
+      v[i] -= dgt[i];                               // exact remainder
+    }
+    uint16_t* A = base + ((int64_t)(0 * TCS + sl) * n + r) * KP;
+    uint16_t* B = base + ((int64_t)((R ? 1 : 2) * TCS + sl) * n + r) * KP;
+    if constexpr (R) {
+      A[lane] = bf16_bits(dgt[0]);
+      A[32 + lane] = bf16_bits(dgt[1]);
+      B[lane] = bf16_bits(MODE ? dgt[1] : dgt[0]);
+      B[32 + lane] = bf16_bits(MODE ? dgt[0] : 0.0);
+    } else {
+      uint16_t* A2 = base + ((int64_t)(1 * TCS + sl) * n + r) * KP;
+      A[lane] = bf16_bits(dgt[0]);
+      A[32 + lane] = bf16_bits(dgt[1]);
+      A[64 + lane] = bf16_bits(dgt[2]);
+      A[96 + lane] = bf16_bits(dgt[3]);
+      A2[lane] = bf16_bits(dgt[1]);
+      A2[32 + lane] = bf16_bits(-dgt[0]);
+      A2[64 + lane] = bf16_bits(dgt[3]);
+      A2[96 + lane] = bf16_bits(-dgt[2]);
+      if (MODE) {
+        B[lane] = bf16_bits(dgt[2]);
+        B[32 + lane] = bf16_bits(dgt[3]);
+        B[64 + lane] = bf16_bits(dgt[0]);
+        B[96 + lane] = bf16_bits(dgt[1]);
+      } else {
+        B[lane] = bf16_bits(dgt[0]);
+        B[32 + lane] = bf16_bits(dgt[1]);
+        B[64 + lane] = bf16_bits(0.0);
+        B[96 + lane] = bf16_bits(0.0);
+      }
+    }
+  }
+}
+
+// One CTA (4 warps) per 128 x 32 tile of C's lower triangle.  All TCS slices of the tile's 32 B rows are
+// staged once; for each A slice s the warps stage its 128 rows (and A' for complex problems), then one
+// thread issues the MMAs of every pair (s, t) with s + t < TCS into the level accumulator s + t in TMEM,
+// commits to an mbarrier, and the warps wait (bounded) before the next stage.  The epilogue reads each
+// level with tcgen05.ld, combines the levels exactly in int64, scales by 2^(e_row + e_col) and subtracts
+// from C.  A wait that runs out marks the problem's status SKN_ERR_CUDA and leaves its C tile unchanged.
+template <bool R>
+__global__ void __launch_bounds__(128) k_r2k_tc(Grp G, Mat Cm, int m) {
+  constexpr int KP = R ? 64 : 128;
+  constexpr uint32_t SBO = (KP / 8) * 128;         // bytes between 8-row groups of a staged tile
+  constexpr int A_BYTES = 128 * KP * 2, B_BYTES = 32 * KP * 2;
+  constexpr int NACC = R ? 1 : 2;                  // accumulators per level (C_r, C_i)
+  constexpr uint32_t TMEM_COLS = R ? 256 : 512;    // TCS levels x NACC x 32 columns, rounded up
+  const int g = blockIdx.y, p = G.prob[g];
+  if (!live(G, p)) return;
+  const int n = G.n;
+  const int nJ = cdiv_d(m, 32);
+  const int I = blockIdx.x / nJ, J = blockIdx.x % nJ;
+  const int r0 = I * 128, c0 = J * 32;
+  if (r0 + 127 < c0) return;                       // entirely above the diagonal
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sB = smem;                              // TCS tiles of 32 rows
+  uint8_t* sA = smem + TCS * B_BYTES;              // A (and A') of one slice, 128 rows
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+  __shared__ double s_cs[32];
+  const WS w = ws_of(G, g);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t bar_a = smem_u32(&bar);
+  if (tid == 0) {
+    s_fail = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid < 32) s_cs[tid] = (c0 + tid < m) ? ldexp(1.0, w.tce[c0 + tid]) : 0.0;
+  // B slices of rows c0 .. c0 + 31 (rows past m are zero)
+  const uint16_t* slB = w.tcs + (int64_t)(R ? 1 : 2) * TCS * n * KP;
+  for (int v = tid; v < TCS * 32 * (KP / 8); v += 128) {
+    const int t = v / (32 * (KP / 8)), rem = v % (32 * (KP / 8));
+    const int r = rem / (KP / 8), g8 = rem % (KP / 8);
+    uint4 x = make_uint4(0u, 0u, 0u, 0u);
+    if (c0 + r < m) x = *reinterpret_cast<const uint4*>(slB + ((int64_t)t * n + c0 + r) * KP + g8 * 8);
+    *reinterpret_cast<uint4*>(sB + t * B_BYTES + (r / 8) * SBO + g8 * 128 + (r % 8) * 16) = x;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_slot;
+  uint32_t phase = 0;
+  for (int sl = 0; sl < TCS; ++sl) {
+    for (int f = 0; f < NACC; ++f) {               // A (f = 0), A' (f = 1) rows r0 .. r0 + 127
+      const uint16_t* slA = w.tcs + ((int64_t)(f * TCS + sl) * n) * KP;
+      for (int v = tid; v < 128 * (KP / 8); v += 128) {
+        const int r = v / (KP / 8), g8 = v % (KP / 8);
+        uint4 x = make_uint4(0u, 0u, 0u, 0u);
+        if (r0 + r < m) x = *reinterpret_cast<const uint4*>(slA + (int64_t)(r0 + r) * KP + g8 * 8);
+        *reinterpret_cast<uint4*>(sA + f * A_BYTES + (r / 8) * SBO + g8 * 128 + (r % 8) * 16) = x;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;");   // the tiles are read by the tensor core (async proxy)
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+      for (int t = 0; t + sl < TCS; ++t) {
+        const uint32_t col = (uint32_t)((sl + t) * NACC * 32);
+#pragma unroll
+        for (int kk = 0; kk < KP / 16; ++kk) {
+          const uint32_t acc = (sl > 0 || kk > 0) ? 1u : 0u;
+          const uint64_t bd = tc_desc(b0 + t * B_BYTES + kk * 256, SBO);
+          tc_mma(tmem + col, tc_desc(a0 + kk * 256, SBO), bd, acc);
+          if (NACC == 2) tc_mma(tmem + col + 32, tc_desc(a0 + A_BYTES + kk * 256, SBO), bd, acc);
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a));
+    }
+    if (!tc_wait(bar_a, phase)) s_fail = 1;
+    phase ^= 1u;
+    __syncthreads();
+    if (s_fail) break;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (!s_fail) {
+    const int row = r0 + warp * 32 + lane;        // this thread's TMEM lane
+    const double rs = (row < m) ? ldexp(1.0, w.tce[row]) : 0.0;
+    double2* C = mat_ptr(G, g, p, Cm);
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int cb = 0; cb < 32; cb += 8) {
+      long long hr[8], lr[8], hi[8], li[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) hr[q] = lr[q] = hi[q] = li[q] = 0;
+#pragma unroll
+      for (int L = 0; L < TCS; ++L) {
+        uint32_t vr[8], vi[8];
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                     : "=r"(vr[0]), "=r"(vr[1]), "=r"(vr[2]), "=r"(vr[3]), "=r"(vr[4]), "=r"(vr[5]), "=r"(vr[6]),
+                       "=r"(vr[7])
+                     : "r"(lane_base + (uint32_t)(L * NACC * 32 + cb)));
+        if (NACC == 2)
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                       : "=r"(vi[0]), "=r"(vi[1]), "=r"(vi[2]), "=r"(vi[3]), "=r"(vi[4]), "=r"(vi[5]), "=r"(vi[6]),
+                         "=r"(vi[7])
+                       : "r"(lane_base + (uint32_t)(L * NACC * 32 + 32 + cb)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        const int sh = (L <= 3) ? 7 * (3 - L) : 7 * (6 - L);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const long long a = (long long)__float2int_rn(__uint_as_float(vr[q])) << sh;
+          if (L <= 3) hr[q] += a; else lr[q] += a;
+          if (NACC == 2) {
+            const long long b = (long long)__float2int_rn(__uint_as_float(vi[q])) << sh;
+            if (L <= 3) hi[q] += b; else li[q] += b;
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int col = c0 + cb + q;
+        if (row < m && col < m && row >= col) {
+          const double sc = rs * s_cs[cb + q];
+          double2* t = C + row + (int64_t)col * n;
+          double2 cv = zld<R>(t);
+          cv.x -= fma((double)hr[q], 0x1p-35, (double)lr[q] * 0x1p-56) * sc;
+          if (NACC == 2) cv.y = (row == col) ? 0.0 : cv.y - fma((double)hi[q], 0x1p-35, (double)li[q] * 0x1p-56) * sc;
+          zst<R>(t, cv);
+        }
+      }
+    }
+  } else if (tid == 0) {
+    G.status[p] = SKN_ERR_CUDA;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
 // ------------------------------------------------------------------ reduction to standard form
@@ -953,11 +1241,19 @@ static_assert(8 * TS <= TS * TLD, "hemv partials fit in the tile's space");
 constexpr int sm_r2k(int mode, int t) { return (mode ? 4 : 2) * KC * t * (int)sizeof(double2); }   // <= 64 KB
 constexpr int sm_gemm(int t) { return 2 * KC * t * (int)sizeof(double2); }
 
+// Dynamic shared memory of k_r2k_tc: the staged slices (real: 45 KB, complex: 120 KB), the real variant padded
+// to 96 KB so that at most two CTAs share an SM, as many as its 256 TMEM columns each allow.
+constexpr int tc_smem(bool real) { return real ? 96 * 1024 : TCS * 32 * 128 * 2 + 2 * 128 * 128 * 2; }
+static_assert(TCS * 32 * 64 * 2 + 128 * 64 * 2 <= 96 * 1024, "real slices fit the padded region");
+constexpr int TC_MIN_M = 512;    // trailing matrices from this size up take the tensor-core update when asked
+
 template <bool R>
 cudaError_t set_attrs() {
   cudaError_t e = cudaFuncSetAttribute(k_rank2k<R, 1, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_r2k(1, 64));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tr_hemv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_HEMV);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_r2k_tc<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem(R));
   return e;
 }
 
@@ -970,8 +1266,13 @@ inline unsigned tri_tiles(int m, int t = TS) {
 inline bool small_tiles(int64_t tiles64, int n_prob, int sms) { return tiles64 * n_prob < 2LL * sms; }
 
 template <bool R, int MODE>
-void rank2k(const Grp& G, Mat C, int m, Mat P, Mat Q, int K, int sms, cudaStream_t st) {
+void rank2k(const Grp& G, Mat C, int m, Mat P, Mat Q, int K, int sms, bool tc, cudaStream_t st) {
   const unsigned Pn = (unsigned)G.n_prob;
+  if (tc && m >= TC_MIN_M) {          // slices of the panel's rows, then the tensor-core tiles
+    k_r2k_split<R, MODE><<<dim3(cdiv(m, 8), Pn), 256, 0, st>>>(G, P, Q, m, K);
+    k_r2k_tc<R><<<dim3((unsigned)(cdiv(m, 128) * cdiv(m, 32)), Pn), 128, tc_smem(R), st>>>(G, C, m);
+    return;
+  }
   if (small_tiles(tri_tiles(m, 64), G.n_prob, sms))
     k_rank2k<R, MODE, 32><<<dim3(tri_tiles(m, 32), Pn), 64, sm_r2k(MODE, 32), st>>>(G, C, m, P, Q, K);
   else
@@ -993,7 +1294,7 @@ void gemm_nn(const Grp& G, int t, int sms, cudaStream_t st) {
 }
 
 template <bool R>
-void run(const Grp& G, cudaStream_t st) {
+void run(const Grp& G, bool tc, cudaStream_t st) {
   const int n = G.n;
   const unsigned P = (unsigned)G.n_prob;
   int dev = 0, sms = 0;
@@ -1010,7 +1311,7 @@ void run(const Grp& G, cudaStream_t st) {
     if (m > 0) {
       k_trsm_right<R><<<dim3(cdiv(m, RC), P), RC, 0, st>>>(G, 1, c0, m);
       rank2k<R, 0>(G, Mat{1, (int64_t)(c0 + NB) * (n + 1)}, m, Mat{1, (c0 + NB) + (int64_t)c0 * n}, Mat{1, 0}, NB,
-                   sms, st);
+                   sms, tc, st);
     }
   }
   // reduction to standard form, the panels' left solves deferred
@@ -1021,7 +1322,7 @@ void run(const Grp& G, cudaStream_t st) {
       k_trsm_right<R><<<dim3(cdiv(m, RC), P), RC, 0, st>>>(G, 0, c0, m);
       k_hemm_half<R><<<dim3(cdiv(m * NB, 256), P), 256, 0, st>>>(G, c0, m);
       rank2k<R, 1>(G, Mat{0, (int64_t)(c0 + NB) * (n + 1)}, m, Mat{0, (c0 + NB) + (int64_t)c0 * n},
-                   Mat{1, (c0 + NB) + (int64_t)c0 * n}, NB, sms, st);
+                   Mat{1, (c0 + NB) + (int64_t)c0 * n}, NB, sms, tc, st);
       k_hemm_half<R><<<dim3(cdiv(m * NB, 256), P), 256, 0, st>>>(G, c0, m);
     }
   }
@@ -1045,7 +1346,7 @@ void run(const Grp& G, cudaStream_t st) {
     const int m2 = M - w;
     if (m2 > 0)
       rank2k<R, 1>(G, Mat{0, (int64_t)(c0 + w) * (n + 1)}, m2, Mat{0, (c0 + w) + (int64_t)c0 * n}, Mat{2, c0 + w}, w,
-                   sms, st);
+                   sms, tc, st);
   }
   k_tri_bounds<R><<<P, 256, 0, st>>>(G);
   k_tri_eig<<<dim3(cdiv(n, 128), P), 128, 0, st>>>(G);
@@ -1060,9 +1361,9 @@ extern "C" int skn_eigh_wide_scratch_bytes(int n_prob, int n, int64_t* bytes) {
   return SKN_OK;
 }
 
-extern "C" int skn_eigh_gen_wide(int n_prob, int n, const int32_t* prob, const int32_t* nvec, const int64_t* hs_off,
-                                 const int64_t* eig_off, double* H, double* S, double* eig, int32_t* status,
-                                 double* scratch, int64_t scratch_bytes, int real, cudaStream_t stream) {
+static int wide_entry(int n_prob, int n, const int32_t* prob, const int32_t* nvec, const int64_t* hs_off,
+                      const int64_t* eig_off, double* H, double* S, double* eig, int32_t* status, double* scratch,
+                      int64_t scratch_bytes, int real, bool tc, cudaStream_t stream) {
   if (n_prob < 0 || n < 1) return SKN_ERR_ARG;
   if (n_prob == 0) return SKN_OK;
   if (n_prob > 32767) return SKN_ERR_CAPACITY;   // grid z of the zero-row scan holds 2 n_prob
@@ -1075,8 +1376,24 @@ extern "C" int skn_eigh_gen_wide(int n_prob, int n, const int32_t* prob, const i
   if ((real ? set_attrs<true>() : set_attrs<false>()) != cudaSuccess) return SKN_ERR_CUDA;
   Grp G{n, n_prob, prob, nvec, hs_off, eig_off, (double2*)H, (double2*)S, eig, status, (double2*)scratch};
   if (real)
-    run<true>(G, stream);
+    run<true>(G, tc, stream);
   else
-    run<false>(G, stream);
+    run<false>(G, tc, stream);
   return cudaPeekAtLastError() == cudaSuccess ? SKN_OK : SKN_ERR_CUDA;
+}
+
+
+extern "C" int skn_eigh_gen_wide(int n_prob, int n, const int32_t* prob, const int32_t* nvec, const int64_t* hs_off,
+                                 const int64_t* eig_off, double* H, double* S, double* eig, int32_t* status,
+                                 double* scratch, int64_t scratch_bytes, int real, cudaStream_t stream) {
+  return wide_entry(n_prob, n, prob, nvec, hs_off, eig_off, H, S, eig, status, scratch, scratch_bytes, real, false,
+                    stream);
+}
+
+extern "C" int skn_eigh_gen_wide_tc(int n_prob, int n, const int32_t* prob, const int32_t* nvec,
+                                    const int64_t* hs_off, const int64_t* eig_off, double* H, double* S, double* eig,
+                                    int32_t* status, double* scratch, int64_t scratch_bytes, int real,
+                                    cudaStream_t stream) {
+  return wide_entry(n_prob, n, prob, nvec, hs_off, eig_off, H, S, eig, status, scratch, scratch_bytes, real, true,
+                    stream);
 }

@@ -451,16 +451,19 @@ KERNELS_PER_CALL = {"skn_bond_counts": 1, "skn_bond_fill": 1, "skn_image_phases"
                     "skn_bloch": 1, "skn_bloch_pairs": 1, "skn_eigh_gen_batched": 1, "skn_eigh_gen_vectors": 2, "skn_fermi_gap": 1,
                     "skn_dos": 2, "skn_eigh_gen_large": 1, "skn_eigh_gen_vectors_noalloc": 2}
 
-def wide_launches(n: int, nb: int = 32, ts: int = 64) -> int:
-    """Kernel launches of one skn_eigh_gen_wide call for problems of n orbitals (its host sequence)."""
+def wide_launches(n: int, nb: int = 32, tc: bool = False, tc_min: int = 512) -> int:
+    """Kernel launches of one skn_eigh_gen_wide(_tc) call for problems of n orbitals (its host sequence);
+    with ``tc`` a rank-2k update of a trailing matrix of ``tc_min`` rows or more is two launches."""
+    def r2k(m):
+        return 2 if (tc and m >= tc_min) else 1
     T = -(-n // nb)
-    k = 3 + T + 2 * (T - 1)                   # set-up; Cholesky: diagonal blocks, row solves + updates
-    k += T + 4 * (T - 1)                      # reduction: diagonal blocks; solve, two hemm, rank-2k
+    k = 3 + T + (T - 1) + sum(r2k(n - c0 - nb) for c0 in range(0, n - nb, nb))    # set-up; Cholesky
+    k += T + 3 * (T - 1) + sum(r2k(n - c0 - nb) for c0 in range(0, n - nb, nb))   # reduction
     k += (T - 1) + sum(1 for t in range(1, T) if (t + 1) * nb < n)   # deferred solves
     c0 = 0
     while c0 < n - 1:                         # tridiagonalisation: 6 per column, 1 per panel update
         w = min(nb, n - 1 - c0)
-        k += 6 * w + (1 if n - c0 - w > 0 else 0)
+        k += 6 * w + (r2k(n - c0 - w) if n - c0 - w > 0 else 0)
         c0 += nb
     return k + 2                              # bounds and eigenvalues
 
@@ -521,7 +524,7 @@ class Engine:
 
     def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None,
                  tuning=None, large_threshold: Optional[int] = 1024, large_cluster: Optional[int] = None,
-                 real_path: bool = True, wide_threshold: Optional[int] = 1024):
+                 real_path: bool = True, wide_threshold: Optional[int] = 1024, wide_tc: bool = False):
         _dev(tables.device)
         self.tables = tables
         self.tuning = tuning          # autotune.Tuning: eigensolver launch shape per problem-size bucket
@@ -532,6 +535,8 @@ class Engine:
         # problems above wide_threshold orbitals run on the device-wide eigensolver instead (route_wide):
         # measured on GB300 it is 4.6x the 4-CTA cluster at n = 1024 and 6-7x at n = 2048-4096
         self.wide_threshold = wide_threshold
+        # the device-wide path's rank-2k updates on the tensor cores (skn_eigh_gen_wide_tc)
+        self.wide_tc = wide_tc
         # values-only solves of problems with exactly real H(k), S(k) use the real-arithmetic
         # kernel (skn_eigh_gen_batched_real): same numbers, a quarter of the FP64 work
         self.real_path = bool(real_path)
@@ -551,7 +556,8 @@ class Engine:
         if ev is not None:
             b.record()
             ev.append((name, a, b))
-        self.launches += wide_launches(args[1]) if name == "skn_eigh_gen_wide" else KERNELS_PER_CALL.get(name, 1)
+        self.launches += (wide_launches(args[1], tc=name.endswith("_tc")) if name.startswith("skn_eigh_gen_wide")
+                          else KERNELS_PER_CALL.get(name, 1))
 
     def run(self, plan: Plan, dos_range=(-10.0, 10.0), dos_points: int = 5000, dos_sigma: float = 0.1,
             dos_window: float = 0.0, keep_hs: bool = False, hs_only: bool = False,
@@ -718,7 +724,8 @@ class Engine:
 
         def launch(gi, sfx, order_g, count, max_n, st):
             if isinstance(sfx, tuple):
-                self._call("skn_eigh_gen_wide", count, max_n, ptr(order_g), ptr(db.n), ptr(db.hs_off), ptr(db.eoff),
+                self._call("skn_eigh_gen_wide_tc" if self.wide_tc else "skn_eigh_gen_wide", count, max_n,
+                           ptr(order_g), ptr(db.n), ptr(db.hs_off), ptr(db.eoff),
                            ptr(Hk), ptr(Sk), ptr(eig), ptr(eig_status), ptr(scratch[gi]),
                            int(scratch[gi].numel() * 8), int(sfx[2]), st)
             elif isinstance(sfx, int):
