@@ -674,7 +674,7 @@ def run_path_only(args):
             "ms_per_execute": 1e3 * t / max(args.steps, 1)}
 
 
-def run_wide_case(spec, steps=1, warmup=1, seed=0, tc=False):
+def run_wide_case(spec, steps=1, warmup=1, seed=0, tc=True):
     """The device-wide eigensolver alone on ``count`` seeded random Hermitian-definite problems of ``n``
     orbitals (spec "n:count"), as one group: ``warmup`` untimed then ``steps`` timed calls, each on fresh
     copies of H and S (the solver works in place).  For profiling and for the rate at a given size; ``tc``
@@ -753,10 +753,11 @@ def run_serving_load(dev, n_requests=2000, rate=20.0, capacity=None, chunk=125):
                            "chunk i from seed 1000 + i, one seeded shuffle"}
 
 
-def run_large_structure(dev):
+def run_large_structure(dev, tc=True):
     """1000-atom Ga/As zincblende supercell (5x5x5 conventional cells, a = 5.65 A, 0.05 A jitter),
     spd on both species (n = 9000), Gamma plus the 7 other points of the 2x2x2 Gamma-centred grid:
-    the whole path once, the eigensolve on the device-wide path."""
+    the whole path once, the eigensolve on the device-wide path (``tc``: its rank-2k updates on the
+    tensor cores)."""
     import torch
     from slakonet_gb300 import engine as E, synthetic as syn
     st = syn.zincblende_supercell()
@@ -766,7 +767,7 @@ def run_large_structure(dev):
     st["weights"] = np.full(8, 1.0 / 8)
     ts = E.TableSet.from_synthetic(tables, sd, dev)
     plan = E.plan_batch([st], ts)
-    eng = E.Engine(ts)
+    eng = E.Engine(ts, wide_tc=tc)
     eng.event_log = []
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -784,9 +785,10 @@ def run_large_structure(dev):
             "eig_status_ok": int((res.eig_status == 0).sum()), "wall_s": wall,
             "phase_s": {k: round(v, 4) for k, v in phases.items()},
             "eigensolve_tflops": flops / eig_s * 1e-12, "gap_eV": float(res.stats[0, E.STAT["gap_ev"]]),
-            "real_k_points": int(real.sum()), "fp64_flops": flops,
-            "note": "all k-points on the device-wide eigensolver (skn_eigh_gen_wide), real arithmetic for the "
-                    "k-points with 2k integer; FP64 count 8/3 n^3 per real and 32/3 n^3 per complex k-point"}
+            "real_k_points": int(real.sum()), "fp64_flops": flops, "tensor_cores": bool(tc),
+            "note": "all k-points on the device-wide eigensolver (skn_eigh_gen_wide_tc with tensor_cores, else "
+                    "skn_eigh_gen_wide), real arithmetic for the k-points with 2k integer; FP64-equivalent count "
+                    "8/3 n^3 per real and 32/3 n^3 per complex k-point"}
 
 
 REF_GPU_STRIDE = 32       # reference GPU path: every 32nd structure by size (8 of the 256)
@@ -1031,10 +1033,13 @@ def main():
                     help="with --path-only: every K-th structure by size (16: the CPU-baseline sample)")
     ap.add_argument("--wide-case", default=None, metavar="N:COUNT",
                     help="time the device-wide eigensolver alone on COUNT random problems of N orbitals")
-    ap.add_argument("--wide-tc", action="store_true",
-                    help="with --wide-case or --large-structure: rank-2k updates on the tensor cores")
-    ap.add_argument("--large-structure", action="store_true",
-                    help="also run the 1000-atom, n = 9000, 8 k-point structure once (about two minutes)")
+    ap.add_argument("--wide-fp64", action="store_true",
+                    help="with --wide-case, --large-structure or --large-only: the device-wide eigensolver's rank-2k "
+                         "updates in FP64 instead of on the tensor cores")
+    ap.add_argument("--no-large-structure", dest="large_structure", action="store_false",
+                    help="skip the 1000-atom, n = 9000, 8 k-point structure (run once by default, about 30 s)")
+    ap.add_argument("--large-only", action="store_true",
+                    help="run only the 1000-atom structure once and print its JSON line with clocks")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -1045,7 +1050,16 @@ def main():
         print(json.dumps(run_path_only(args)))
         return
     if args.wide_case:
-        print(json.dumps(run_wide_case(args.wide_case, args.steps, args.warmup, tc=args.wide_tc)))
+        print(json.dumps(run_wide_case(args.wide_case, args.steps, args.warmup, tc=not args.wide_fp64)))
+        return
+    if args.large_only:
+        import torch
+        import __graft_entry__ as ge
+        ge.build()
+        with ClockSampler(0) as clk:
+            out = run_large_structure(torch.device("cuda", 0), tc=not args.wide_fp64)
+        out["clocks"] = clk.summary()
+        print(json.dumps(out))
         return
     if args.impl == "reference":
         if rank == 0:
@@ -1084,7 +1098,7 @@ def main():
         if world == 1 and args.large_structure:
             import torch
             log("large structure")
-            out["large_structure"] = run_large_structure(torch.device("cuda", 0))
+            out["large_structure"] = run_large_structure(torch.device("cuda", 0), tc=not args.wide_fp64)
         if world == 1 and not args.no_reference_gpu:
             log("reference per-structure GPU path and training step (subprocess)")
             out.update(run_reference_gpu_subprocess(args))

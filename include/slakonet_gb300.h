@@ -134,13 +134,17 @@ int skn_bloch(int n_prob, const int32_t* prob_struct, const int32_t* prob_k, con
 
 /*
  * The same Bloch sums organised by atom pair: a warp per (ordered atom pair,
- * chunk of 16 k-points), its lanes over (k-point, block element), so warps
+ * chunk of 8 k-points), its lanes over (k-point, block element), so warps
  * stay full when blocks are small (1x1, 1x4, 4x4 orbitals) and a small cell's
- * many k-points spread over many warps.  Values are bitwise those of
- * skn_bloch.  Replaces the same reference code as skn_bloch.
+ * many k-points spread over many warps; the warps of a CTA take the adjacent
+ * row blocks of one column block, so columns are written in long runs.
+ * Values are bitwise those of skn_bloch.  Replaces the same reference code as
+ * skn_bloch.
  *   n_struct               structures
- *   n_units, unit_base[n_struct]   work units: structure s owns N_s^2 * ceil(nk_s / 16)
- *                          of them, numbered from unit_base[s] (exclusive prefix sum)
+ *   n_units, unit_base[n_struct]   work units, numbered from unit_base[s]
+ *                          (exclusive prefix sum): structure s owns
+ *                          ceil(nk_s / 8) * N_s^2 of them with lower = 0 and
+ *                          ceil(nk_s / 8) * N_s (N_s + 1) / 2 with lower = 1
  *   k_ptr[n_struct+1]      problem index of each structure's first k-point (problems
  *                          of a structure are consecutive, k-point order)
  *   lower                  1: write only the entries on or below the diagonal (what the

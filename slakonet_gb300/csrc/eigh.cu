@@ -964,6 +964,7 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
       if (j < n) {
         const double lam = w[j];
         double u1 = d[0] - lam, u2 = (n > 1) ? e[0] : 0.0;
+        double rmax = 0.0;                 // largest |1 / pivot|
         for (int i = 0; i < n - 1; ++i) {
           const double c = e[i];
           const double a1 = d[i + 1] - lam;
@@ -982,6 +983,7 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
             u2 = -m * b1;
           }
           s_ru1[i * VNT + tid] = 1.0 / r1;
+          rmax = fmax(rmax, fabs(1.0 / r1));
           s_u2[i * VNT + tid] = r2;
           s_u3[i * VNT + tid] = r3;
           s_m[i * VNT + tid] = m;
@@ -989,8 +991,17 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
         }
         if (fabs(u1) < pivmin) u1 = (u1 < 0.0) ? -pivmin : pivmin;
         s_ru1[(n - 1) * VNT + tid] = 1.0 / u1;
+        rmax = fmax(rmax, fabs(1.0 / u1));
+        // A lam exact to the last bit (the Newton step can land on the eigenvalue) leaves a pivot at the
+        // 1e-300 floor, and a solve then grows the vector by up to 1 / pivot: its sum of squares overflowed
+        // and the eigenvector came out NaN.  Every solve's right-hand side is therefore scaled by
+        // ysc = 2^-e with 2^e >= rmax, which keeps the solution near unit size; a power of two scales
+        // exactly, so without a tiny pivot the normalised vectors are bitwise what they were unscaled.
+        int rex = 0;
+        frexp(rmax, &rex);
+        const double ysc = rex > 0 ? ldexp(1.0, -rex) : 1.0;
         // y lives in the real parts of column j of Y
-        for (int i = 0; i < n; ++i) Y[(int64_t)i * n + j] = make_double2(hash_unit(j, i), 0.0);
+        for (int i = 0; i < n; ++i) Y[(int64_t)i * n + j] = make_double2(hash_unit(j, i) * ysc, 0.0);
         for (int it = 0; it < 2; ++it) {
           for (int i = 0; i < n - 1; ++i) {
             const double m = s_m[i * VNT + tid];
@@ -1011,7 +1022,12 @@ __global__ void __launch_bounds__(VNT) k_eigvec(int n_prob, const int32_t* __res
             x2 = x1;
             x1 = xi;
           }
-          const double inv = 1.0 / sqrt(nrm);
+          if (!(nrm > 0.0 && nrm <= 1.7976931348623157e308)) {   // vanished, overflowed or NaN: restart from e_j
+            for (int i = 0; i < n; ++i) Y[(int64_t)i * n + j].x = (i == j) ? ysc : 0.0;
+            nrm = ysc * ysc;
+          }
+          // normalised, and scaled by ysc again when it is the next solve's right-hand side
+          const double inv = (it == 0 ? ysc : 1.0) / sqrt(nrm);
           for (int i = 0; i < n; ++i) Y[(int64_t)i * n + j].x *= inv;
         }
       }

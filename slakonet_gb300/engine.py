@@ -401,7 +401,7 @@ class BatchResult:
         return self.eig[o: o + int(p.nk[s]) * int(p.nb[s])].view(int(p.nk[s]), int(p.nb[s]))
 
 
-BLOCH_KCHUNK = 16          # k-points per work unit of skn_bloch_pairs (csrc/bloch.cu)
+BLOCH_KCHUNK = 8           # k-points per work unit of skn_bloch_pairs (csrc/bloch.cu)
 
 
 class DeviceBatch:
@@ -436,11 +436,17 @@ class DeviceBatch:
         self.kwoff = _i64(plan.kw_off, dev)
         self.kw = _f64(plan.kweights, dev)
         self.ne = _f64(plan.nelec, dev)
-        # work units of the Bloch-sum kernel: N_s^2 atom pairs x ceil(nk_s / BLOCH_KCHUNK) k-chunks per structure
-        units = np.diff(plan.atom_ptr).astype(np.int64) ** 2 * ((plan.nk.astype(np.int64) + BLOCH_KCHUNK - 1)
-                                                                 // BLOCH_KCHUNK)
-        self.bloch_units = int(units.sum())
-        self.bloch_unit_base = _i64(np.concatenate([[0], np.cumsum(units)[:-1]]) if len(units) else np.zeros(1), dev)
+        # work units of the Bloch-sum kernel per structure: ceil(nk_s / BLOCH_KCHUNK) k-chunks times the
+        # N_s^2 ordered atom pairs (full matrices) or the N_s (N_s + 1) / 2 pairs on or below the diagonal
+        # (lower triangles), numbered from an exclusive prefix sum
+        na = np.diff(plan.atom_ptr).astype(np.int64)
+        kch = (plan.nk.astype(np.int64) + BLOCH_KCHUNK - 1) // BLOCH_KCHUNK
+
+        def base(units):
+            return _i64(np.concatenate([[0], np.cumsum(units)[:-1]]) if len(units) else np.zeros(1), dev), \
+                int(units.sum())
+        self.bloch_unit_base, self.bloch_units = base(na * na * kch)
+        self.bloch_unit_base_lower, self.bloch_units_lower = base(na * (na + 1) // 2 * kch)
 
     def h2d_bytes(self) -> int:
         return sum(int(v.numel() * v.element_size()) for v in vars(self).values() if isinstance(v, torch.Tensor))
@@ -524,7 +530,7 @@ class Engine:
 
     def __init__(self, tables: TableSet, cutoff: float = CUTOFF_BOHR, stream: Optional[torch.cuda.Stream] = None,
                  tuning=None, large_threshold: Optional[int] = 1024, large_cluster: Optional[int] = None,
-                 real_path: bool = True, wide_threshold: Optional[int] = 1024, wide_tc: bool = False):
+                 real_path: bool = True, wide_threshold: Optional[int] = 1024, wide_tc: bool = True):
         _dev(tables.device)
         self.tables = tables
         self.tuning = tuning          # autotune.Tuning: eigensolver launch shape per problem-size bucket
@@ -535,7 +541,8 @@ class Engine:
         # problems above wide_threshold orbitals run on the device-wide eigensolver instead (route_wide):
         # measured on GB300 it is 4.6x the 4-CTA cluster at n = 1024 and 6-7x at n = 2048-4096
         self.wide_threshold = wide_threshold
-        # the device-wide path's rank-2k updates on the tensor cores (skn_eigh_gen_wide_tc)
+        # the device-wide path's rank-2k updates on the tensor cores (skn_eigh_gen_wide_tc): measured on
+        # GB300, the 1000-atom structure (n = 9000, 8 real k-points) solves in 13.9 s instead of 18.9 s
         self.wide_tc = wide_tc
         # values-only solves of problems with exactly real H(k), S(k) use the real-arithmetic
         # kernel (skn_eigh_gen_batched_real): same numbers, a quarter of the FP64 work
@@ -647,11 +654,13 @@ class Engine:
         Hk = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
         Sk = torch.empty(2 * max(plan.hs_total, 1), dtype=torch.float64, device=dev)
         # the eigensolvers read only the lower triangles; full matrices only when they are returned
-        self._call("skn_bloch_pairs", S, db.bloch_units, ptr(db.bloch_unit_base), ptr(db.kptr), ptr(db.hs_off),
+        lower = 0 if (keep_hs or hs_only) else 1
+        self._call("skn_bloch_pairs", S, db.bloch_units_lower if lower else db.bloch_units,
+                   ptr(db.bloch_unit_base_lower if lower else db.bloch_unit_base), ptr(db.kptr), ptr(db.hs_off),
                    ptr(db.atom_ptr),
                    ptr(db.orb_ptr), ptr(db.aoff), ptr(db.norb), ptr(db.pair_base), ptr(d_pair_ptr), ptr(bond_img),
                    ptr(bond_blk), ptr(blk_H), ptr(blk_S), ptr(db.rng), ptr(db.phb), ptr(phases), ptr(db.onsite),
-                   0 if (keep_hs or hs_only) else 1, ptr(Hk), ptr(Sk), stream)
+                   lower, ptr(Hk), ptr(Sk), stream)
         self._status = status
         hs_copy = (Hk.clone(), Sk.clone()) if keep_hs else (None, None)
         if hs_only:

@@ -51,7 +51,8 @@ def _old(plan, db, b, phases, blk_H, blk_S, stream):
 def _pairs(plan, db, b, phases, blk_H, blk_S, stream, lower, fill):
     H = torch.full((2 * plan.hs_total,), fill, dtype=torch.float64, device=DEV)
     S = torch.full_like(H, fill)
-    call("skn_bloch_pairs", plan.n_struct, db.bloch_units, ptr(db.bloch_unit_base), ptr(db.kptr), ptr(db.hs_off),
+    units, unit_base = (db.bloch_units_lower, db.bloch_unit_base_lower) if lower else (db.bloch_units, db.bloch_unit_base)
+    call("skn_bloch_pairs", plan.n_struct, units, ptr(unit_base), ptr(db.kptr), ptr(db.hs_off),
          ptr(db.atom_ptr),
          ptr(db.orb_ptr), ptr(db.aoff), ptr(db.norb), ptr(db.pair_base), ptr(b["pair_ptr"]), ptr(b["bond_img"]),
          ptr(b["bond_blk"]), ptr(blk_H), ptr(blk_S), ptr(db.rng), ptr(db.phb), ptr(phases), ptr(db.onsite),

@@ -75,3 +75,27 @@ def test_with_eigenvectors_drop_in_layout():
                                                        get_fermi=True, device=DEV, with_eigenvectors=True)
     ev = props["calc"].eigenvectors
     assert ev.shape == (1, 18, 18, 8) and ev.dtype == torch.complex128
+
+
+def test_eigenvectors_finite_where_the_eigenvalue_is_exact():
+    """A 5-atom cell of the 64-structure fitting batch (n = 35, 200 k-points) whose eigenvalues the Sturm/Newton
+    step finds to the last bit at some k-points: T - e I then has a zero pivot, and inverse iteration must still
+    return finite, S-orthonormal eigenvectors (with a 1e-300 pivot floor one solve overflowed to NaN)."""
+    from slakonet_gb300 import training as T
+    batch = T.fitting_batch(64, seed=0)
+    st = batch[38]
+    sd = syn.default_shell_dict()
+    zs = sorted({int(z) for s in batch for z in s["numbers"]})     # the batch's tables (one seeded draw)
+    tables = syn.make_tables(zs, sd, seed=0)
+    sdz = {z: sd[z] for z in zs}
+    ts = E.TableSet.from_synthetic(tables, sdz, DEV)
+    plan = E.plan_batch([st], ts)
+    res = E.Engine(ts).run(plan, vectors=True)
+    C = res.eigenvectors(0)
+    assert bool(torch.isfinite(torch.view_as_real(C)).all())
+    k = np.asarray(st["kpoints"])
+    sub = {key: v for key, v in st.items() if key != "weights"}      # _check sets its own k-points
+    r, o, d = _check(sub, tables, sdz, k[np.linspace(0, len(k) - 1, 24).astype(int)])
+    print(f"fitting-batch cell (n = {int(plan.nb[0])}, {len(k)} k): all {len(k)} k-points finite; "
+          f"residual {r:.1e}, orthonormality {o:.1e}, direction {d:.1e}")
+    assert r <= 1e-10 and o <= 1e-10 and d <= 1e-8

@@ -50,7 +50,7 @@ def test_gaas_1000_atoms_n9000_eight_kpoints():
     eig_s = sum(a.elapsed_time(b) for name, a, b in eng.event_log if name == "eigensolve") * 1e-3
     real = plan.prob_real if plan.prob_real is not None else np.zeros(8, dtype=bool)
     flops = float(np.sum(np.where(real, 8.0 / 3.0, 32.0 / 3.0) * plan.prob_n.astype(np.float64) ** 3))
-    print(f"eigensolve: {eig_s:.2f} s, {flops / eig_s * 1e-12:.3f} TFLOP/s FP64 "
+    print(f"eigensolve: {eig_s:.2f} s, {flops / eig_s * 1e-12:.3f} TFLOP/s FP64-equivalent "
           f"({int(real.sum())} of 8 k-points real; 8/3 n^3 per real, 32/3 n^3 per complex k-point)")
     assert (res.eig_status.cpu().numpy() == 0).all()
     n = 9000
