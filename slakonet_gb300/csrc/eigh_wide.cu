@@ -44,6 +44,17 @@ constexpr int TLD = TS + 1;            // leading dimension of the staged hemv t
 constexpr int TCS = 7;                 // integer slices per operand row in the tensor-core update
 
 SKN_DEVINL int cdiv_d(int a, int b) { return (a + b - 1) / b; }
+// Rows of each slice array of the tensor-core update: n rounded up to whole 128-row tiles, so a tile's block
+// of rows never ends past the array.
+__host__ __device__ inline int64_t tc_rows(int n) { return ((int64_t)n + 127) / 128 * 128; }
+// Element index of (row r, column k) in a slice array with kp columns, in the tensor cores' K-major
+// core-matrix order: 8-row groups of kp * 8 elements, each a run of 8 x 8 core matrices (8 rows x 16 bytes)
+// along K.  A 128-row (or 32-row) block starting at a multiple of 8 is one contiguous run in exactly the
+// order the MMA's shared-memory descriptor reads (LBO 128 bytes, SBO kp * 16 bytes), so it is staged by a
+// single bulk copy.
+SKN_DEVINL int64_t tc_idx(int r, int k, int kp) {
+  return (int64_t)(r >> 3) * (8 * kp) + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
+}
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 
 // ------------------------------------------------------------------ arithmetic (R: real parts only)
@@ -120,7 +131,7 @@ __host__ __device__ inline Lay layout(int n) {
   L.d32 = take(o, (n + 3) / 4);
   L.e232 = take(o, (n + 3) / 4);
   L.flg = take(o, (2 * (int64_t)n + 3) / 4);
-  L.tcs = take(o, (int64_t)3 * TCS * n * 128 * 2 / 16);   // bf16 slices of the tensor-core update (A, A', B)
+  L.tcs = take(o, (int64_t)3 * TCS * tc_rows(n) * 128 * 2 / 16);   // bf16 slices of the tensor-core update
   L.tce = take(o, ((int64_t)n + 3) / 4);                    // their row exponents
   L.stride = o;
   return L;
@@ -131,7 +142,7 @@ struct WS {
   double *d, *e2, *rd;
   float *d32, *e232;
   int* flg;
-  uint16_t* tcs;   // bf16 slices: [form][TCS][n][KP], form 0 A (A_r), 1 A' (A_i, complex), 2 B
+  uint16_t* tcs;   // bf16 slices: [form][TCS][tc_rows(n) x KP in tc_idx order], form 0 A, 1 A' (complex), 2 B
   int* tce;        // row exponents of the sliced rows
 };
 
@@ -504,7 +515,11 @@ __global__ void __launch_bounds__(256) k_r2k_split(Grp G, Mat Pm, Mat Qm, int m,
   double v[4];
 #pragma unroll
   for (int i = 0; i < NSEC; ++i) v[i] = ldexp(x[i], -ex);   // exact
+  const int64_t np = tc_rows(n);
   uint16_t* base = w.tcs;
+  int64_t ix[NSEC];                                 // this lane's columns of row r: lane, 32 + lane, ...
+#pragma unroll
+  for (int i = 0; i < NSEC; ++i) ix[i] = tc_idx(r, 32 * i + lane, KP);
   for (int sl = 0; sl < TCS; ++sl) {
     double dgt[4];
 #pragma unroll
@@ -513,44 +528,59 @@ __global__ void __launch_bounds__(256) k_r2k_split(Grp G, Mat Pm, Mat Qm, int m,
       dgt[i] = rint(v[i]);                          // |dgt| <= 128, then <= 64
       v[i] -= dgt[i];                               // exact remainder
     }
-    uint16_t* A = base + ((int64_t)(0 * TCS + sl) * n + r) * KP;
-    uint16_t* B = base + ((int64_t)((R ? 1 : 2) * TCS + sl) * n + r) * KP;
+    uint16_t* A = base + (int64_t)(0 * TCS + sl) * np * KP;
+    uint16_t* B = base + (int64_t)((R ? 1 : 2) * TCS + sl) * np * KP;
     if constexpr (R) {
-      A[lane] = bf16_bits(dgt[0]);
-      A[32 + lane] = bf16_bits(dgt[1]);
-      B[lane] = bf16_bits(MODE ? dgt[1] : dgt[0]);
-      B[32 + lane] = bf16_bits(MODE ? dgt[0] : 0.0);
+      A[ix[0]] = bf16_bits(dgt[0]);
+      A[ix[1]] = bf16_bits(dgt[1]);
+      B[ix[0]] = bf16_bits(MODE ? dgt[1] : dgt[0]);
+      B[ix[1]] = bf16_bits(MODE ? dgt[0] : 0.0);
     } else {
-      uint16_t* A2 = base + ((int64_t)(1 * TCS + sl) * n + r) * KP;
-      A[lane] = bf16_bits(dgt[0]);
-      A[32 + lane] = bf16_bits(dgt[1]);
-      A[64 + lane] = bf16_bits(dgt[2]);
-      A[96 + lane] = bf16_bits(dgt[3]);
-      A2[lane] = bf16_bits(dgt[1]);
-      A2[32 + lane] = bf16_bits(-dgt[0]);
-      A2[64 + lane] = bf16_bits(dgt[3]);
-      A2[96 + lane] = bf16_bits(-dgt[2]);
+      uint16_t* A2 = base + (int64_t)(1 * TCS + sl) * np * KP;
+      A[ix[0]] = bf16_bits(dgt[0]);
+      A[ix[1]] = bf16_bits(dgt[1]);
+      A[ix[2]] = bf16_bits(dgt[2]);
+      A[ix[3]] = bf16_bits(dgt[3]);
+      A2[ix[0]] = bf16_bits(dgt[1]);
+      A2[ix[1]] = bf16_bits(-dgt[0]);
+      A2[ix[2]] = bf16_bits(dgt[3]);
+      A2[ix[3]] = bf16_bits(-dgt[2]);
       if (MODE) {
-        B[lane] = bf16_bits(dgt[2]);
-        B[32 + lane] = bf16_bits(dgt[3]);
-        B[64 + lane] = bf16_bits(dgt[0]);
-        B[96 + lane] = bf16_bits(dgt[1]);
+        B[ix[0]] = bf16_bits(dgt[2]);
+        B[ix[1]] = bf16_bits(dgt[3]);
+        B[ix[2]] = bf16_bits(dgt[0]);
+        B[ix[3]] = bf16_bits(dgt[1]);
       } else {
-        B[lane] = bf16_bits(dgt[0]);
-        B[32 + lane] = bf16_bits(dgt[1]);
-        B[64 + lane] = bf16_bits(0.0);
-        B[96 + lane] = bf16_bits(0.0);
+        B[ix[0]] = bf16_bits(dgt[0]);
+        B[ix[1]] = bf16_bits(dgt[1]);
+        B[ix[2]] = bf16_bits(0.0);
+        B[ix[3]] = bf16_bits(0.0);
       }
     }
   }
 }
 
-// One CTA (4 warps) per 128 x 32 tile of C's lower triangle.  All TCS slices of the tile's 32 B rows are
-// staged once; for each A slice s the warps stage its 128 rows (and A' for complex problems), then one
-// thread issues the MMAs of every pair (s, t) with s + t < TCS into the level accumulator s + t in TMEM,
-// commits to an mbarrier, and the warps wait (bounded) before the next stage.  The epilogue reads each
-// level with tcgen05.ld, combines the levels exactly in int64, scales by 2^(e_row + e_col) and subtracts
-// from C.  A wait that runs out marks the problem's status SKN_ERR_CUDA and leaves its C tile unchanged.
+// Bulk copy of `bytes` contiguous bytes from global to this CTA's shared memory, completing on `bar`
+// (complete_tx); both addresses 16-byte aligned, bytes a multiple of 16.
+SKN_DEVINL void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+SKN_DEVINL void bar_expect(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// One CTA (4 warps) per 128 x 32 tile of C's lower triangle.  Thread 0 runs a two-stage pipeline: the TCS
+// slices of the tile's 32 B rows and the first two slices of its 128 A rows (and A' for complex problems)
+// arrive by bulk copies, each one contiguous block of the slice arrays (their tc_idx order is the MMA's
+// shared-memory layout); for each A slice s, once its copy has landed, thread 0 issues the MMAs of every
+// pair (s, t) with s + t < TCS into the level accumulator s + t in TMEM and commits them to that stage's
+// mbarrier, and when those MMAs are done it refills the stage with slice s + 2, so copies overlap the MMAs
+// of the other stage.  All waits are bounded.  The epilogue reads each level with tcgen05.ld, combines the
+// levels exactly in int64, scales by 2^(e_row + e_col) and subtracts from C.  A wait that runs out marks
+// the problem's status SKN_ERR_CUDA and leaves its C tile unchanged; thread 0 then still waits (bounded)
+// for every copy and MMA it issued before the CTA frees its TMEM and exits.
 template <bool R>
 __global__ void __launch_bounds__(128) k_r2k_tc(Grp G, Mat Cm, int m) {
   constexpr int KP = R ? 64 : 128;
@@ -567,17 +597,17 @@ __global__ void __launch_bounds__(128) k_r2k_tc(Grp G, Mat Cm, int m) {
   if (r0 + 127 < c0) return;                       // entirely above the diagonal
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sB = smem;                              // TCS tiles of 32 rows
-  uint8_t* sA = smem + TCS * B_BYTES;              // A (and A') of one slice, 128 rows
-  __shared__ __align__(8) uint64_t bar;
+  uint8_t* sA = smem + TCS * B_BYTES;              // 2 stages x NACC tiles of 128 rows
+  // 0: B slices landed; 1, 2: stage 0 / 1 landed; 3, 4: the MMAs reading stage 0 / 1 are done
+  __shared__ __align__(8) uint64_t bars[5];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail;
   __shared__ double s_cs[32];
   const WS w = ws_of(G, g);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t bar_a = smem_u32(&bar);
   if (tid == 0) {
     s_fail = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a));
+    for (int b = 0; b < 5; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[b])));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   if (warp == 0) {
@@ -586,52 +616,72 @@ __global__ void __launch_bounds__(128) k_r2k_tc(Grp G, Mat Cm, int m) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid < 32) s_cs[tid] = (c0 + tid < m) ? ldexp(1.0, w.tce[c0 + tid]) : 0.0;
-  // B slices of rows c0 .. c0 + 31 (rows past m are zero)
-  const uint16_t* slB = w.tcs + (int64_t)(R ? 1 : 2) * TCS * n * KP;
-  for (int v = tid; v < TCS * 32 * (KP / 8); v += 128) {
-    const int t = v / (32 * (KP / 8)), rem = v % (32 * (KP / 8));
-    const int r = rem / (KP / 8), g8 = rem % (KP / 8);
-    uint4 x = make_uint4(0u, 0u, 0u, 0u);
-    if (c0 + r < m) x = *reinterpret_cast<const uint4*>(slB + ((int64_t)t * n + c0 + r) * KP + g8 * 8);
-    *reinterpret_cast<uint4*>(sB + t * B_BYTES + (r / 8) * SBO + g8 * 128 + (r % 8) * 16) = x;
-  }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_slot;
-  uint32_t phase = 0;
-  for (int sl = 0; sl < TCS; ++sl) {
-    for (int f = 0; f < NACC; ++f) {               // A (f = 0), A' (f = 1) rows r0 .. r0 + 127
-      const uint16_t* slA = w.tcs + ((int64_t)(f * TCS + sl) * n) * KP;
-      for (int v = tid; v < 128 * (KP / 8); v += 128) {
-        const int r = v / (KP / 8), g8 = v % (KP / 8);
-        uint4 x = make_uint4(0u, 0u, 0u, 0u);
-        if (r0 + r < m) x = *reinterpret_cast<const uint4*>(slA + (int64_t)(r0 + r) * KP + g8 * 8);
-        *reinterpret_cast<uint4*>(sA + f * A_BYTES + (r / 8) * SBO + g8 * 128 + (r % 8) * 16) = x;
-      }
-    }
-    asm volatile("fence.proxy.async.shared::cta;");   // the tiles are read by the tensor core (async proxy)
-    __syncthreads();
-    if (tid == 0) {
+  if (tid == 0) {
+    const int64_t np = tc_rows(n);
+    const uint16_t* slices = w.tcs;
+    auto slice = [&](int f, int sl) { return slices + (int64_t)(f * TCS + sl) * np * KP; };
+    const uint32_t bar_b = smem_u32(&bars[0]);
+    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+    auto load_stage = [&](int st, int sl) {
+      const uint32_t bar = smem_u32(&bars[1 + st]);
+      bar_expect(bar, NACC * A_BYTES);
+      for (int f = 0; f < NACC; ++f)
+        bulk_g2s(a0 + (uint32_t)((st * NACC + f) * A_BYTES), slice(f, sl) + (int64_t)r0 * KP, A_BYTES, bar);
+    };
+    bar_expect(bar_b, TCS * B_BYTES);
+    for (int t = 0; t < TCS; ++t)
+      bulk_g2s(b0 + (uint32_t)(t * B_BYTES), slice(R ? 1 : 2, t) + (int64_t)c0 * KP, B_BYTES, bar_b);
+    load_stage(0, 0);
+    load_stage(1, 1);
+    // armed[b]: phases of mbarrier b armed (copies issued or MMAs committed) and not yet waited for
+    int armed[5] = {1, 1, 1, 0, 0};
+    int done[5] = {0, 0, 0, 0, 0};              // phases waited for
+    bool ok = tc_wait(bar_b, 0);
+    if (ok) done[0] = 1;
+    for (int sl = 0; ok && sl < TCS; ++sl) {
+      const int st = sl & 1;
+      ok = tc_wait(smem_u32(&bars[1 + st]), (uint32_t)(done[1 + st] & 1));
+      if (!ok) break;
+      ++done[1 + st];
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+      const uint32_t as = a0 + (uint32_t)(st * NACC * A_BYTES);
       for (int t = 0; t + sl < TCS; ++t) {
         const uint32_t col = (uint32_t)((sl + t) * NACC * 32);
 #pragma unroll
         for (int kk = 0; kk < KP / 16; ++kk) {
           const uint32_t acc = (sl > 0 || kk > 0) ? 1u : 0u;
           const uint64_t bd = tc_desc(b0 + t * B_BYTES + kk * 256, SBO);
-          tc_mma(tmem + col, tc_desc(a0 + kk * 256, SBO), bd, acc);
-          if (NACC == 2) tc_mma(tmem + col + 32, tc_desc(a0 + A_BYTES + kk * 256, SBO), bd, acc);
+          tc_mma(tmem + col, tc_desc(as + kk * 256, SBO), bd, acc);
+          if (NACC == 2) tc_mma(tmem + col + 32, tc_desc(as + A_BYTES + kk * 256, SBO), bd, acc);
         }
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a));
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&bars[3 + st])));
+      ++armed[3 + st];
+      if (sl + 2 < TCS) {                         // refill this stage once its MMAs have read it
+        ok = tc_wait(smem_u32(&bars[3 + st]), (uint32_t)(done[3 + st] & 1));
+        if (!ok) break;
+        ++done[3 + st];
+        load_stage(st, sl + 2);
+        ++armed[1 + st];
+      }
     }
-    if (!tc_wait(bar_a, phase)) s_fail = 1;
-    phase ^= 1u;
-    __syncthreads();
-    if (s_fail) break;
+    // every copy and MMA issued must have completed before the epilogue reads TMEM or the CTA exits
+    for (int b = 0; b < 5; ++b)
+      while (done[b] < armed[b]) {
+        if (!tc_wait(smem_u32(&bars[b]), (uint32_t)(done[b] & 1))) {
+          ok = false;
+          break;
+        }
+        ++done[b];
+      }
+    if (!ok) s_fail = 1;
   }
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (!s_fail) {
     const int row = r0 + warp * 32 + lane;        // this thread's TMEM lane
@@ -1241,10 +1291,12 @@ static_assert(8 * TS <= TS * TLD, "hemv partials fit in the tile's space");
 constexpr int sm_r2k(int mode, int t) { return (mode ? 4 : 2) * KC * t * (int)sizeof(double2); }   // <= 64 KB
 constexpr int sm_gemm(int t) { return 2 * KC * t * (int)sizeof(double2); }
 
-// Dynamic shared memory of k_r2k_tc: the staged slices (real: 45 KB, complex: 120 KB), the real variant padded
-// to 96 KB so that at most two CTAs share an SM, as many as its 256 TMEM columns each allow.
-constexpr int tc_smem(bool real) { return real ? 96 * 1024 : TCS * 32 * 128 * 2 + 2 * 128 * 128 * 2; }
-static_assert(TCS * 32 * 64 * 2 + 128 * 64 * 2 <= 96 * 1024, "real slices fit the padded region");
+// Dynamic shared memory of k_r2k_tc: the B slices and two stages of A slices (real: 60 KB, complex: 184 KB),
+// the real variant padded to 96 KB so that at most two CTAs share an SM, as many as its 256 TMEM columns each
+// allow.
+constexpr int tc_smem(bool real) { return real ? 96 * 1024 : TCS * 32 * 128 * 2 + 2 * 2 * 128 * 128 * 2; }
+static_assert(TCS * 32 * 64 * 2 + 2 * 128 * 64 * 2 <= 96 * 1024, "real slices fit the padded region");
+static_assert(TCS * 32 * 128 * 2 + 2 * 2 * 128 * 128 * 2 <= 227 * 1024, "complex slices fit shared memory");
 constexpr int TC_MIN_M = 512;    // trailing matrices from this size up take the tensor-core update when asked
 
 template <bool R>

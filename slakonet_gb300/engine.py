@@ -542,7 +542,7 @@ class Engine:
         # measured on GB300 it is 4.6x the 4-CTA cluster at n = 1024 and 6-7x at n = 2048-4096
         self.wide_threshold = wide_threshold
         # the device-wide path's rank-2k updates on the tensor cores (skn_eigh_gen_wide_tc): measured on
-        # GB300, the 1000-atom structure (n = 9000, 8 real k-points) solves in 13.9 s instead of 18.9 s
+        # GB300, the 1000-atom structure (n = 9000, 8 real k-points) solves in 13.2 s instead of 18.9 s
         self.wide_tc = wide_tc
         # values-only solves of problems with exactly real H(k), S(k) use the real-arithmetic
         # kernel (skn_eigh_gen_batched_real): same numbers, a quarter of the FP64 work
