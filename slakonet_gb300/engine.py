@@ -229,6 +229,55 @@ def _check_index_range(n_at, orb_cum, nk, orb_ptr64) -> None:
                          "exceeds 2^31 eigenvalues")
 
 
+def _checked_arrays(structures: Sequence[dict], cutoff: float):
+    """check_structure for a whole batch: the per-structure loop only converts arrays and compares lengths;
+    finiteness, singular cells and the translation boxes are computed once over the stacked arrays.  When
+    anything looks wrong, the structures are checked one by one instead, so the first bad one raises
+    check_structure's own error."""
+    S = len(structures)
+    nums, pos, cells, kp, kw = [], [], [], [], []
+    try:
+        for st in structures:
+            z = np.asarray(st["numbers"], dtype=np.int64).reshape(-1)
+            p = np.asarray(st["positions"], dtype=np.float64).reshape(-1, 3)
+            c = np.asarray(st["cell"], dtype=np.float64).reshape(3, 3)
+            k = np.asarray(st["kpoints"], dtype=np.float64).reshape(-1, 3)
+            w = np.asarray(st["weights"] if "weights" in st else np.full(len(k), 1.0 / max(len(k), 1)),
+                           dtype=np.float64).reshape(-1)
+            if len(z) == 0 or len(p) != len(z) or len(k) == 0 or len(w) != len(k):
+                raise ValueError
+            nums.append(z)
+            pos.append(p)
+            cells.append(c)
+            kp.append(k)
+            kw.append(w)
+        n_at = np.array([len(z) for z in nums], np.int64)
+        C = np.stack(cells)
+        P = np.concatenate(pos)
+        ok = np.isfinite(C).all() and np.isfinite(P).all() and all(np.isfinite(k).all() for k in kp) and \
+            all(np.isfinite(w).all() for w in kw)
+        if not ok:
+            raise ValueError
+        det = np.linalg.det(C)
+        if (np.abs(det) <= 1e-12 * np.maximum(np.abs(C).reshape(S, -1).max(1), 1.0) ** 3).any():
+            raise ValueError
+        inv = np.linalg.inv(C)
+        first = np.concatenate([[0], np.cumsum(n_at)[:-1]])
+        frac = np.einsum("ai,aij->aj", P, np.repeat(inv, n_at, axis=0))
+        spread = np.maximum.reduceat(frac, first, axis=0) - np.minimum.reduceat(frac, first, axis=0)
+        blen = np.linalg.norm(inv, axis=1)
+        rng = (np.floor(cutoff * blen + spread) + 1).astype(np.int32)
+        n_img = np.prod(2 * rng.astype(np.int64) + 1, axis=1)
+        if (n_img > MAX_IMAGES).any() or (n_img * n_at ** 2 > MAX_PAIR_IMAGES).any():
+            raise ValueError
+    except (ValueError, KeyError, TypeError, IndexError, np.linalg.LinAlgError):
+        # one structure at a time: the first bad one raises its own error
+        out = [check_structure(st, cutoff, s) for s, st in enumerate(structures)]
+        nums, pos, cells, kp, kw, r = (list(x) for x in zip(*out))
+        rng = np.array(r, np.int32).reshape(S, 3)
+    return nums, pos, cells, kp, kw, rng
+
+
 def image_range(cell: np.ndarray, positions: np.ndarray, cutoff: float) -> np.ndarray:
     """Half-widths r of the translation box holding every bond shorter than cutoff.
 
@@ -292,20 +341,9 @@ def plan_batch(structures: Sequence[dict], tables: TableSet, cutoff: float = CUT
     S = len(structures)
     if S == 0:
         raise ValueError("empty batch: no structures")
-    nums, pos, cells, kp, kw = [], [], [], [], []
-    n_at = np.zeros(S, np.int64)
-    nk = np.zeros(S, np.int32)
-    rng = np.zeros((S, 3), np.int32)
-    for s, st in enumerate(structures):
-        z, p, c, k, w, r = check_structure(st, cutoff, s)
-        nums.append(z)
-        pos.append(p)
-        cells.append(c)
-        kp.append(k)
-        kw.append(w)
-        n_at[s] = len(z)
-        nk[s] = len(k)
-        rng[s] = r
+    nums, pos, cells, kp, kw, rng = _checked_arrays(structures, cutoff)
+    n_at = np.array([len(z) for z in nums], np.int64)
+    nk = np.array([len(k) for k in kp], np.int32)
     zall = np.concatenate(nums) if S else np.zeros(0, np.int64)
     lut = tables.__dict__.get("_species_lut")
     if lut is None:
