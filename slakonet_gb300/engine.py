@@ -787,12 +787,18 @@ class Engine:
         if len(groups) == 1:
             launch(0, *groups[0], stream)
             return
-        # one launch per group (cluster group first, then shapes by problem size) on forked streams
+        # one launch per group (in _groups' order) on forked streams.  Replaying a CUDA graph dispatches
+        # these independent branches last-captured first (measured on GB300: capturing the uneven batch's
+        # groups in launch order gave 840-850 ms eigensolves, in reverse order 720-730 ms), so under
+        # capture they are issued in reverse.
         main = torch.cuda.current_stream(self.device)
         fork = torch.cuda.Event()
         fork.record(main)
         joins = []
-        for gi, g in enumerate(groups):
+        seq = list(enumerate(groups))
+        if torch.cuda.is_current_stream_capturing():
+            seq.reverse()
+        for gi, g in seq:
             st = self._side_streams(len(groups))[gi]
             st.wait_event(fork)
             with torch.cuda.stream(st):
@@ -835,10 +841,10 @@ class Engine:
                   else np.zeros(len(wn), dtype=bool))
             for n_, r_ in sorted({(int(a), bool(b)) for a, b in zip(wn, wr)}, reverse=True):
                 sel = plan.order[wide][(wn == n_) & (wr == r_)]
-                out.append((("wide", n_, int(r_)), _i32(sel, self.device), len(sel), n_))
+                out.append((("wide", n_, int(r_)), sel, len(sel), n_))
         for c in sorted(set(csize[csize > 0].tolist()), reverse=True):    # one launch per cluster size
             sel = plan.order[csize == c]
-            out.append((int(c), _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))
+            out.append((int(c), sel, len(sel), int(plan.prob_n[sel].max())))
         small_order = plan.order[~large]
         if len(small_order):
             tuning = self.tuning if self.tuning is not None else _default_tuning()
@@ -848,9 +854,22 @@ class Engine:
             shapes = np.array(shapes, dtype=object)
             for sfx in dict.fromkeys(shapes.tolist()):
                 sel = small_order[shapes == sfx]
-                out.append((sfx, _i32(sel, self.device), len(sel), int(plan.prob_n[sel].max())))
+                out.append((sfx, sel, len(sel), int(plan.prob_n[sel].max())))
         if len(out) == 1 and out[0][0] == "" and out[0][2] == len(plan.order):
             out = []     # the default launch over the batch's own order
+        # Launch order.  The groups run concurrently, each a persistent grid that takes every SM slot it
+        # can get, so a group whose CTAs reach the SMs second waits for the first group's CTAs to drain.
+        # The group that must not wait is the one with a few long problems (on the benchmark batch, the ~100
+        # real problems of up to 492 orbitals): started last they end ~130 ms after everything else.  So
+        # groups go by their largest problem's cost per problem in the group (n^3, x4 when complex) divided
+        # by the group's size: few long problems first, the many small ones last.
+        real = plan.prob_real if (self.real_path and plan.prob_real is not None) else np.zeros(len(plan.prob_n), bool)
+
+        def urgency(g):
+            cost = plan.prob_n[g[1]].astype(np.float64) ** 3 * np.where(real[g[1]], 1.0, 4.0)
+            return -float(cost.max()) / len(g[1])
+        out.sort(key=urgency)
+        out = [(sh, _i32(sel, self.device), cnt, mx) for sh, sel, cnt, mx in out]     # problem lists on the device
         db._groups = (key, out)
         return out
 
