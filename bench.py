@@ -426,7 +426,29 @@ def run_gpu(args, rank, world):
     # that holds the rest of the path (phases, SK blocks, Bloch sums, the persistent eigensolver launches,
     # Fermi/gap, DOS)
     log("graph capture")
-    cap = E.CapturedPath(eng, db, **kw)
+    # The eigensolver groups are independent branches of the graph, and the order in which a replay
+    # dispatches them is not fixed by the capture: on GB300 one instance of this graph replays the batch's
+    # eigensolve in ~700 ms, another in ~820 ms (the ~100 long real problems then start after the complex
+    # grid has taken the SMs).  As the autotuner does for launch policies, three instances are captured,
+    # each is timed over three replays, and the fastest is kept for the timed region.
+    cap, graph_trials = None, []
+    for _ in range(GRAPH_TRIALS):
+        c = E.CapturedPath(eng, db, **kw)
+        tr = []
+        for _ in range(3):
+            eng.bonds(db, out=c.bonds)
+            ga, gb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ga.record()
+            c.replay()
+            gb.record()
+            torch.cuda.synchronize()
+            tr.append(ga.elapsed_time(gb))
+        graph_trials.append(round(statistics.median(tr), 1))
+        if cap is None or graph_trials[-1] < min(graph_trials[:-1]):
+            cap = c
+        else:
+            del c
+        torch.cuda.empty_cache()
     for _ in range(args.warmup):
         eng.bonds(db, out=cap.bonds)
         cap.replay()
@@ -504,7 +526,8 @@ def run_gpu(args, rank, world):
                    "eig_launch_shapes": {str(k): (v or "_t128") for k, v in tuning.choice.items()},
                    "graph": f"value: per step the neighbour list (2 launches, 1 device->host read) then one replay "
                             f"of the captured CUDA graph of the rest of the path ({cap.kernels_per_replay} kernel "
-                            f"launches per replay); uncaptured, the same steps take "
+                            f"launches per replay; the fastest of {GRAPH_TRIALS} captured instances, median replay "
+                            f"ms {graph_trials}); uncaptured, the same steps take "
                             f"{1e3 * elapsed_u / args.steps:.1f} ms",
                    "autotune_s": round(t_tune, 1),
                    "autotune_batch_trials_ms": tuning.timings.get("batch_trials_ms")},
@@ -792,6 +815,7 @@ def run_large_structure(dev, tc=True):
 
 
 REF_GPU_STRIDE = 32       # reference GPU path: every 32nd structure by size (8 of the 256)
+GRAPH_TRIALS = 3          # captured instances of the path's CUDA graph tried before the timed region
 
 
 def run_reference_gpu(dev, sts, tables, sd, stride=REF_GPU_STRIDE, limit=8):

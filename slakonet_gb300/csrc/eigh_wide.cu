@@ -30,6 +30,7 @@
 // code on the real parts only (problems whose H(k), S(k) are exactly real).
 #include <cuda_bf16.h>
 
+#include "exact_round.cuh"
 #include "skn_common.cuh"
 #include "sturm.cuh"
 
@@ -578,7 +579,8 @@ SKN_DEVINL void bar_expect(uint32_t bar, uint32_t bytes) {
 // pair (s, t) with s + t < TCS into the level accumulator s + t in TMEM and commits them to that stage's
 // mbarrier, and when those MMAs are done it refills the stage with slice s + 2, so copies overlap the MMAs
 // of the other stage.  All waits are bounded.  The epilogue reads each level with tcgen05.ld, combines the
-// levels exactly in int64, scales by 2^(e_row + e_col) and subtracts from C.  A wait that runs out marks
+// levels exactly in int64, rounds once to FP64 with the scale 2^(e_row + e_col) (exact_to_double) and
+// subtracts from C.  A wait that runs out marks
 // the problem's status SKN_ERR_CUDA and leaves its C tile unchanged; thread 0 then still waits (bounded)
 // for every copy and MMA it issued before the CTA frees its TMEM and exits.
 template <bool R>
@@ -602,7 +604,7 @@ __global__ void __launch_bounds__(128) k_r2k_tc(Grp G, Mat Cm, int m) {
   __shared__ __align__(8) uint64_t bars[5];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail;
-  __shared__ double s_cs[32];
+  __shared__ int s_ce[32];
   const WS w = ws_of(G, g);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
@@ -615,7 +617,7 @@ __global__ void __launch_bounds__(128) k_r2k_tc(Grp G, Mat Cm, int m) {
                  "r"(TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid < 32) s_cs[tid] = (c0 + tid < m) ? ldexp(1.0, w.tce[c0 + tid]) : 0.0;
+  if (tid < 32) s_ce[tid] = (c0 + tid < m) ? w.tce[c0 + tid] : 0;
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
@@ -685,7 +687,7 @@ __global__ void __launch_bounds__(128) k_r2k_tc(Grp G, Mat Cm, int m) {
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (!s_fail) {
     const int row = r0 + warp * 32 + lane;        // this thread's TMEM lane
-    const double rs = (row < m) ? ldexp(1.0, w.tce[row]) : 0.0;
+    const int re = (row < m) ? w.tce[row] - 56 : 0;   // the level sums count units of 2^(e_row + e_col - 56)
     double2* C = mat_ptr(G, g, p, Cm);
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     for (int cb = 0; cb < 32; cb += 8) {
@@ -720,11 +722,11 @@ __global__ void __launch_bounds__(128) k_r2k_tc(Grp G, Mat Cm, int m) {
       for (int q = 0; q < 8; ++q) {
         const int col = c0 + cb + q;
         if (row < m && col < m && row >= col) {
-          const double sc = rs * s_cs[cb + q];
+          const int e = re + s_ce[cb + q];
           double2* t = C + row + (int64_t)col * n;
           double2 cv = zld<R>(t);
-          cv.x -= fma((double)hr[q], 0x1p-35, (double)lr[q] * 0x1p-56) * sc;
-          if (NACC == 2) cv.y = (row == col) ? 0.0 : cv.y - fma((double)hi[q], 0x1p-35, (double)li[q] * 0x1p-56) * sc;
+          cv.x -= exact_to_double(hr[q], lr[q], e);
+          if (NACC == 2) cv.y = (row == col) ? 0.0 : cv.y - exact_to_double(hi[q], li[q], e);
           zst<R>(t, cv);
         }
       }

@@ -787,18 +787,12 @@ class Engine:
         if len(groups) == 1:
             launch(0, *groups[0], stream)
             return
-        # one launch per group (in _groups' order) on forked streams.  Replaying a CUDA graph dispatches
-        # these independent branches last-captured first (measured on GB300: capturing the uneven batch's
-        # groups in launch order gave 840-850 ms eigensolves, in reverse order 720-730 ms), so under
-        # capture they are issued in reverse.
+        # one launch per group (in _groups' order) on forked streams
         main = torch.cuda.current_stream(self.device)
         fork = torch.cuda.Event()
         fork.record(main)
         joins = []
-        seq = list(enumerate(groups))
-        if torch.cuda.is_current_stream_capturing():
-            seq.reverse()
-        for gi, g in seq:
+        for gi, g in enumerate(groups):
             st = self._side_streams(len(groups))[gi]
             st.wait_event(fork)
             with torch.cuda.stream(st):
