@@ -933,7 +933,7 @@ def run_reference_gpu_subprocess(args) -> dict:
         return {"reference_gpu_path": {"unavailable": f"worker exited {r.returncode}"}}
 
 
-def north_star_ratios(out: dict) -> dict:
+def speedup_targets(out: dict) -> dict:
     """The two speed-up targets against the reference's own code on the same GPU:
     ``vs_plain_gpu``: k-point solves/s of this path over the reference's per-structure GPU path
     (target >= 10x), on the full batch and on the reference's sample alone;
@@ -1126,7 +1126,7 @@ def main():
         if world == 1 and not args.no_reference_gpu:
             log("reference per-structure GPU path and training step (subprocess)")
             out.update(run_reference_gpu_subprocess(args))
-            out.update(north_star_ratios(out))
+            out.update(speedup_targets(out))
         if world == 1 and not args.no_cpu_baseline:
             log("cpu baseline and parity of the timed step")
             out["cpu_baseline"], out["parity"] = run_cpu_baseline(args, gpu_res)
