@@ -546,6 +546,22 @@ def _default_tuning():
     return Tuning.default()
 
 
+def launch_order(groups: Sequence[np.ndarray], prob_n: np.ndarray, prob_real: np.ndarray) -> List[int]:
+    """Order in which the eigensolver's groups (arrays of problem indices) are launched.
+
+    The groups run concurrently, each a persistent grid that takes every SM slot it can get, so a group
+    whose CTAs reach the SMs second waits for the first group's CTAs to drain.  The group that must not
+    wait is the one with a few long problems (on the benchmark batch, the ~100 real problems of up to 492
+    orbitals): started last, they end ~130 ms after everything else.  So groups go by their largest
+    problem's cost (n^3, x4 when complex) divided by the group's size: few long problems first, the many
+    small ones last; ties keep the given order."""
+    def urgency(i):
+        sel = groups[i]
+        cost = prob_n[sel].astype(np.float64) ** 3 * np.where(prob_real[sel], 1.0, 4.0)
+        return -float(cost.max()) / len(sel)
+    return sorted(range(len(groups)), key=urgency)
+
+
 def route_large(prob_n: np.ndarray, threshold: Optional[int] = 1024, cluster: Optional[int] = None) -> np.ndarray:
     """Cluster size per problem, 0 for the one-CTA-per-problem eigensolver.
 
@@ -851,18 +867,8 @@ class Engine:
                 out.append((sfx, sel, len(sel), int(plan.prob_n[sel].max())))
         if len(out) == 1 and out[0][0] == "" and out[0][2] == len(plan.order):
             out = []     # the default launch over the batch's own order
-        # Launch order.  The groups run concurrently, each a persistent grid that takes every SM slot it
-        # can get, so a group whose CTAs reach the SMs second waits for the first group's CTAs to drain.
-        # The group that must not wait is the one with a few long problems (on the benchmark batch, the ~100
-        # real problems of up to 492 orbitals): started last they end ~130 ms after everything else.  So
-        # groups go by their largest problem's cost per problem in the group (n^3, x4 when complex) divided
-        # by the group's size: few long problems first, the many small ones last.
         real = plan.prob_real if (self.real_path and plan.prob_real is not None) else np.zeros(len(plan.prob_n), bool)
-
-        def urgency(g):
-            cost = plan.prob_n[g[1]].astype(np.float64) ** 3 * np.where(real[g[1]], 1.0, 4.0)
-            return -float(cost.max()) / len(g[1])
-        out.sort(key=urgency)
+        out = [out[i] for i in launch_order([g[1] for g in out], plan.prob_n, real)]
         out = [(sh, _i32(sel, self.device), cnt, mx) for sh, sel, cnt, mx in out]     # problem lists on the device
         db._groups = (key, out)
         return out

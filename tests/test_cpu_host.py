@@ -311,3 +311,19 @@ def test_index_range_guard_rejects_int32_overflow():
     with pytest.raises(ValueError, match="batch too large"):
         E._check_index_range(n_at, np.array([0, 2 ** 31], np.int64), np.array([1, 1], np.int32),
                              np.array([0, 1, 2], np.int64))
+
+
+def test_eigensolver_groups_launch_few_long_problems_first():
+    """The ~100 long real problems of the uneven batch go before the complex groups' full grids, and the many
+    small problems last; the order depends on cost per problem in the group, not on the groups' input order."""
+    n = np.array([492, 480, 300, 128, 100, 64, 40] * 10)
+    real = np.zeros(len(n), bool)
+    real[:2] = True                                                      # two long real problems
+    idx = np.arange(len(n))
+    big_real = idx[:2]
+    big_complex = idx[(n >= 300) & ~real]
+    small_complex = idx[(n < 300)]
+    for groups in ([small_complex, big_complex, big_real], [big_complex, big_real, small_complex]):
+        order = E.launch_order(groups, n, real)
+        assert [groups[i] is big_real for i in order] == [True, False, False]
+        assert groups[order[-1]] is small_complex
