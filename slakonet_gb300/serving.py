@@ -40,9 +40,18 @@ from .model import MultiElementSkfParameterOptimizer, properties_dict
 MAX_N = E.LARGE_MAX_N   # cluster eigensolver bound (csrc/eigh_cluster.cu)
 
 
-def request_bytes(n_orb: int, nk: int, dos_points: int) -> int:
-    """Device bytes one request holds while in flight (H, S, eigenvalues, DOS, slack for bonds)."""
-    return int(2 * 16 * n_orb * n_orb * nk + 8 * n_orb * nk + 8 * dos_points + (8 << 20))
+def request_bytes(n_orb: int, nk: int, dos_points: int, wide_threshold: Optional[int] = None) -> int:
+    """Device bytes one request holds while in flight (H, S, eigenvalues, DOS, slack for bonds), plus the
+    device-wide eigensolver's scratch when its problems are above ``wide_threshold`` orbitals (panels,
+    partial sums and the tensor-core update's integer slices: about 5.5 KB per orbital and k-point)."""
+    nb = int(2 * 16 * n_orb * n_orb * nk + 8 * n_orb * nk + 8 * dos_points + (8 << 20))
+    if wide_threshold is not None and wide_threshold < n_orb <= MAX_N and nk > 0:
+        import ctypes
+        from . import _lib
+        need = ctypes.c_int64(0)
+        _lib.call("skn_eigh_wide_scratch_bytes", nk, n_orb, ctypes.addressof(need))
+        nb += int(need.value)
+    return nb
 
 
 @dataclass
@@ -134,8 +143,8 @@ class Server:
         nk = len(structure["kpoints"])
         with self.cv:
             self.rid += 1
-            req = Request(self.rid, structure, n_orb, nk, request_bytes(n_orb, nk, self.dos["dos_points"]),
-                          time.perf_counter())
+            req = Request(self.rid, structure, n_orb, nk,
+                          request_bytes(n_orb, nk, self.dos["dos_points"], self.wide_threshold), time.perf_counter())
         err = None
         if missing:
             err = ValueError(f"no shells for element Z={missing[0]}")

@@ -255,3 +255,16 @@ def test_size_lanes_keep_large_requests_off_the_small_lane_and_take_the_cheapest
             assert max(n) <= 256
         assert cost == sorted(cost)
     assert any(max(n) > 256 for w, _, n in taken if w == 2)
+
+
+def test_admission_counts_the_device_wide_scratch():
+    """A request whose problems run on the device-wide eigensolver also holds that solver's scratch while in
+    flight; below the threshold the estimate is H, S, eigenvalues and DOS alone."""
+    import ctypes
+    from slakonet_gb300 import _lib
+    base = SV.request_bytes(1300, 5, 1000)
+    assert SV.request_bytes(1300, 5, 1000, wide_threshold=2000) == base
+    need = ctypes.c_int64(0)
+    _lib.call("skn_eigh_wide_scratch_bytes", 5, 1300, ctypes.addressof(need))
+    assert need.value > 0
+    assert SV.request_bytes(1300, 5, 1000, wide_threshold=512) == base + need.value
