@@ -276,6 +276,7 @@ class MultiElementSkfParameterOptimizer(nn.Module):
         data = torch.load(path, map_location="cpu", weights_only=False)
         meta, sd, skm = data["metadata"], data["trained_parameters"], data["skf_metadata"]
         m = cls()
+        m.skf_directory = meta.get("skf_directory")
         for pk in meta["available_pairs"]:
             h, s = {}, {}
             for key, v in sd.items():
@@ -284,10 +285,51 @@ class MultiElementSkfParameterOptimizer(nn.Module):
                 elif key.startswith(f"skf_optimizers.{pk}.s_params."):
                     s[key.split(".")[-1]] = v
             md = skm[pk]
-            m.skf_optimizers[pk] = SkfParameterOptimizer(md["atom_pair"], h, s, md["grid"], md.get("atomic_data"),
-                                                         md.get("hs_cutoff"))
+            opt = SkfParameterOptimizer(md["atom_pair"], h, s, md["grid"], md.get("atomic_data"), md.get("hs_cutoff"))
+            # the rest of the pair's metadata travels unchanged to save_ultra_compact
+            opt.skf_dict.update({k: v for k, v in md.items()
+                                 if k not in ("hamiltonian", "overlap", "atom_pair", "grid", "hs_cutoff")})
+            m.skf_optimizers[pk] = opt
         m.load_state_dict(sd, strict=False)
         return m
+
+    def save_ultra_compact(self, path) -> str:
+        """Write the reference's ultra-compact checkpoint (slakonet/optim.py:485-519), the file
+        ``load_ultra_compact`` reads here and in the reference: ``metadata`` (pairs and elements),
+        ``trained_parameters`` (the state dict: after fitting, the fitted values) and ``skf_metadata`` (each
+        pair's grid, cutoff and atomic data, without the tables the state dict already holds).  Only
+        tensors, numbers, strings, lists and dicts are stored, so ``torch.load(..., weights_only=True)`` --
+        what the reference's loader does under current PyTorch -- reads it.  The suffix becomes ``.pt``, as in
+        the reference; returns the path written."""
+        root, ext = os.path.splitext(os.fspath(path))
+        out = root + ".pt"
+        os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
+
+        def plain(v):
+            if isinstance(v, np.ndarray):
+                return torch.as_tensor(v.copy())
+            if isinstance(v, np.generic):
+                return v.item()
+            if isinstance(v, torch.Tensor):
+                return v.detach().cpu().clone()
+            if isinstance(v, dict):
+                return {k: plain(x) for k, x in v.items()}
+            if isinstance(v, (list, tuple)):
+                return [plain(x) for x in v]
+            return v
+        pairs = list(self.skf_optimizers.keys())
+        elems = sorted({int(z) for opt in self.skf_optimizers.values() for z in opt.atom_pair})
+        data = {
+            "metadata": {"skf_directory": getattr(self, "skf_directory", None), "elements_in_system": elems,
+                         "element_pairs": [[int(z) for z in opt.atom_pair] for opt in self.skf_optimizers.values()],
+                         "available_pairs": pairs, "class_name": "MultiElementSkfParameterOptimizer",
+                         "ultra_compact": True},
+            "trained_parameters": {k: v.detach().cpu().clone() for k, v in self.state_dict().items()},
+            "skf_metadata": {pk: plain({k: v for k, v in opt.skf_dict.items() if k not in ("hamiltonian", "overlap")})
+                             for pk, opt in self.skf_optimizers.items()},
+        }
+        torch.save(data, out)
+        return out
 
     def get_updated_skfs(self):
         """Per-pair dicts of live parameters (the data ``Skf.from_dict`` would wrap)."""
