@@ -90,3 +90,54 @@ def train_step(model: MultiElementSkfParameterOptimizer, optimizer: torch.optim.
     return {"loss": float(loss.detach()), "batch_loss": float(batch_loss.detach()), "forward_s": t1 - t0,
             "structures_used": int(ok.sum()),
             "backward_s": t2 - t1, "degenerate_pairs": int(st.get("degenerate_pairs", 0))}
+
+
+def fit(model: MultiElementSkfParameterOptimizer, structures: Sequence[dict], dos_target: torch.Tensor,
+        gap_target: torch.Tensor, shell_dict, device, num_epochs: int = 100, learning_rate: float = 1e-5,
+        batch_size: Optional[int] = None, save_directory: Optional[str] = None, early_stopping_patience: int = 20,
+        seed: int = 0, log=None) -> Dict[str, object]:
+    """The reference's fitting loop (``train_multi_vasp_skf_parameters``, slakonet/optim.py:1570-1855) around
+    ``train_step``: AdamW at ``learning_rate``; ReduceLROnPlateau (factor 0.8, patience 10) stepped with each
+    epoch's loss; each epoch on all structures, or on ``batch_size`` of them drawn at random (seeded); the
+    best model so far kept and, with ``save_directory``, written as ``best_model.pt`` in the reference's
+    ultra-compact checkpoint format; a stop after ``early_stopping_patience`` epochs without improvement;
+    the final model and the loss history (``final_model.pt``, ``training_history.json``) at the end.  The
+    reference reads its targets from VASP runs; here they are passed in (DOS ``[S, 1000]`` and gaps ``[S]``
+    in eV, as ``perturbed_targets`` makes).  Returns the history and the best loss."""
+    import json
+    import os
+    optimizer = torch.optim.AdamW(model.parameters(), lr=learning_rate)
+    scheduler = torch.optim.lr_scheduler.ReduceLROnPlateau(optimizer, mode="min", factor=0.8, patience=10)
+    rng = np.random.default_rng(seed)
+    history: List[dict] = []
+    best_loss, best_epoch, stale = float("inf"), -1, 0
+    best_state = None
+    if save_directory:
+        os.makedirs(save_directory, exist_ok=True)
+    for epoch in range(num_epochs):
+        if batch_size is not None and batch_size < len(structures):
+            idx = np.sort(rng.choice(len(structures), size=batch_size, replace=False))
+        else:
+            idx = np.arange(len(structures))
+        sel = torch.as_tensor(idx, device=dos_target.device)
+        rec = train_step(model, optimizer, [structures[i] for i in idx], dos_target[sel], gap_target[sel],
+                         shell_dict, device, scheduler=scheduler)
+        loss = rec["loss"]
+        history.append({"epoch": epoch, "loss": loss, "lr": optimizer.param_groups[0]["lr"],
+                        "structures": int(rec.get("structures_used", len(idx)))})
+        if log is not None:
+            log(history[-1])
+        if loss < best_loss:
+            best_loss, best_epoch, stale = loss, epoch, 0
+            best_state = {k: v.detach().clone() for k, v in model.state_dict().items()}
+            if save_directory:
+                model.save_ultra_compact(os.path.join(save_directory, "best_model.pt"))
+        else:
+            stale += 1
+        if stale >= early_stopping_patience:
+            break
+    if save_directory:
+        model.save_ultra_compact(os.path.join(save_directory, "final_model.pt"))
+        with open(os.path.join(save_directory, "training_history.json"), "w") as f:
+            json.dump({"history": history, "best_loss": best_loss, "best_epoch": best_epoch}, f, indent=1)
+    return {"history": history, "best_loss": best_loss, "best_epoch": best_epoch, "best_state": best_state}

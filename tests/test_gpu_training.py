@@ -84,3 +84,22 @@ def test_train_steps_follow_the_reference_loop():
         assert worst_g <= 1e-9
         assert worst_p <= REL
         assert worst_small <= 1e-3 * lr
+
+
+def test_fit_loop_on_the_gpu_writes_a_checkpoint_the_loader_reads(tmp_path):
+    """Three epochs of ``training.fit`` on three cells of the 64-structure fitting batch, targets from 5 %
+    perturbed amplitudes: finite losses, and the best model written in the reference's checkpoint format
+    reads back with the parameters it held."""
+    sts = T.fitting_batch(64, seed=0)[:3]
+    zs = sorted({int(z) for st in sts for z in st["numbers"]})
+    sd = syn.default_shell_dict()
+    tables = syn.make_tables(zs, {z: sd[z] for z in zs}, seed=0)
+    model = M.MultiElementSkfParameterOptimizer.from_tables(tables).to(DEV)
+    dos_t, gap_t = T.perturbed_targets(tables, sts, sd, DEV, rel=0.05, seed=1)
+    out = T.fit(model, sts, dos_t, gap_t, sd, DEV, num_epochs=3, learning_rate=1e-4, save_directory=str(tmp_path))
+    losses = [h["loss"] for h in out["history"]]
+    print(f"fit: losses {losses}")
+    assert len(losses) == 3 and all(np.isfinite(losses))
+    best = M.MultiElementSkfParameterOptimizer.load_ultra_compact(str(tmp_path / "best_model.pt"))
+    for k, v in best.state_dict().items():
+        assert torch.equal(v, out["best_state"][k].cpu()), k
