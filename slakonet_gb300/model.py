@@ -83,6 +83,49 @@ def mp_kpoints(mesh) -> np.ndarray:
     return np.stack(np.meshgrid(a, b, c, indexing="ij"), -1).reshape(-1, 3)
 
 
+def reduce_time_reversal(kpoints, weights=None, tol: float = 1e-9):
+    """Halve a k-point list by time reversal: ``(k_red, w_red, index)``.
+
+    The real-space blocks H(T), S(T) are real, so H(-k) and S(-k) are the complex conjugates of H(k) and
+    S(k), and the eigenvalues at -k equal those at k.  Of each pair {k, -k modulo reciprocal lattice
+    vectors} found in the list, the first stays in ``k_red`` with the pair's weights summed; a k-point that
+    is its own partner (2k integer: Gamma and zone-boundary points) or whose partner is absent stays with
+    its own weight.  ``index[i]`` is the row of ``k_red`` whose eigenvalues are k-point i's, so
+    ``eig_red[index]`` restores the full list's eigenvalues, and the reduced list with ``w_red`` gives the
+    full list's Fermi level, gap and DOS (the same eigenvalues with the same total weight) for about half
+    the eigensolves on Monkhorst-Pack and Gamma-centred grids.  The reference solves every k-point.  Partner
+    eigenvalues agree to rounding (the partner's phases come from -k or from 1 - k, which round differently)."""
+    k = np.asarray(kpoints, dtype=np.float64).reshape(-1, 3)
+    nk = len(k)
+    w = np.full(nk, 1.0 / max(nk, 1)) if weights is None else np.asarray(weights, dtype=np.float64).reshape(-1)
+    if len(w) != nk:
+        raise ValueError(f"{len(w)} weights for {nk} k-points")
+    scale = 1.0 / tol
+    period = int(round(scale))
+
+    def key(v):
+        q = np.mod(np.round(v * scale).astype(np.int64), period)
+        return tuple(int(x) for x in q)
+    first = {}
+    for i in range(nk):
+        first.setdefault(key(k[i]), []).append(i)
+    index = np.full(nk, -1, np.int64)
+    keep, wk = [], []
+    for i in range(nk):
+        if index[i] >= 0:
+            continue
+        index[i] = len(keep)
+        keep.append(i)
+        wsum = w[i]
+        for j in first.get(key(-k[i]), []):
+            if j != i and index[j] < 0:
+                index[j] = index[i]
+                wsum += w[j]
+                break
+        wk.append(wsum)
+    return k[keep].copy(), np.array(wk, dtype=np.float64), index
+
+
 def klines_kpoints(klines) -> np.ndarray:
     """Band-path points ``k1 + i (k2-k1)/(N-1)`` per segment (slakonet/atoms.py:448-502)."""
     kl = np.asarray(torch.as_tensor(klines).detach().cpu().numpy(), dtype=np.float64).reshape(-1, 7)
